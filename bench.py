@@ -1,0 +1,411 @@
+"""Benchmark of the TeaLeaf implicit solve on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload ppcg4096|cheby4096|cg4096|cg512]
+
+A step is one TeaLeaf timestep (one tea_leaf call: set-up, the solve to
+tl_eps, finalise) of a synthetic five-state problem with the reference's
+deck layout.  The default workload is 4096^2 cells, PPCG with the 4-row
+block-Jacobi preconditioner, 10 inner steps, halo depth 2, 20 CG steps
+before the switch, tl_eps 1e-15, FP64.  W untimed steps run first (the
+first contains the CG steps and the eigenvalue estimate); K steps are timed
+with CUDA events on the library's stream.
+
+value : cell-iterations/s (interior cells x outer solver iterations / s)
+        with the fields resident in HBM, through the library's fastest
+        driver mode.
+e2e   : the same metric through the per-call C ABI (two host round trips
+        per CG iteration, as the reference's Fortran makes them), with each
+        step's input fields (density, energy1) copied host->device from
+        pinned memory and the result field (energy1) copied back inside the
+        timed region.
+--impl reference times the CPU restatement of the reference (oracle/) on
+the host cores on bounded samples of the same workload; see the design doc.
+
+Multi-GPU (torchrun): every rank solves its own copy of the problem
+(replicas; the solve is not sharded), value = all ranks' cell-iterations /
+max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (cells, solver, prec, halo, inner, presteps, eps, dominant kernel,
+    #        algorithmic bytes per cell of one launch of it)
+    "ppcg4096": (4096, "ppcg", "jac_block", 2, 10, 20, 1e-15,
+                 "tea_leaf_ppcg_solve_update_r", 56),
+    "cheby4096": (4096, "chebyshev", "jac_block", 2, 10, 20, 1e-15,
+                  "tea_leaf_cheby_solve_calc_p", 72),
+    "cg4096": (4096, "cg", "jac_block", 2, 10, 20, 1e-15,
+               "tea_leaf_cg_solve_calc_ur", 64),
+    "cg512": (512, "cg", "jac_diag", 1, 10, 25, 1e-15,
+              "tea_leaf_cg_solve_calc_ur", 64),
+}
+
+
+def deck_for(name, steps):
+    from tealeaf_opencl_gb300 import decks
+    cells, solver, prec, halo, inner, presteps, eps = WORKLOADS[name][:7]
+    # tl_ch_cg_epslim large: the switch to Chebyshev/PPCG happens right after
+    # the tl_ch_cg_presteps CG steps that estimate the eigenvalues
+    extra = "tl_ch_cg_epslim=1.0e300" if solver in ("ppcg", "chebyshev") else ""
+    return decks.five_state_deck(cells, solver=solver, prec=prec, steps=steps,
+                                 eps=eps, max_iters=5000, halo=halo,
+                                 inner_steps=inner, presteps=presteps,
+                                 summary_frequency=0, extra=extra)
+
+
+def config_for(name):
+    cells, solver, prec, halo, inner, presteps, eps = WORKLOADS[name][:7]
+    cfg = {"workload": "%s: %dx%d five-state TeaLeaf, %s + %s, FP64, tl_eps %g"
+                       % (name, cells, cells, solver, prec, eps),
+           "cells": cells * cells, "solver": solver, "preconditioner": prec,
+           "halo_depth": halo, "tl_eps": eps, "dt": 0.004,
+           "domain": "[0,10]^2, five reference states",
+           "l2": "inputs larger than L2: each FP64 field is %.0f MB, the "
+                 "solve touches about 12 of them" % (cells * cells * 8 / 1e6),
+           "parallelism": "replicas"}
+    if solver == "ppcg":
+        cfg["inner_steps"] = inner
+    if solver in ("ppcg", "chebyshev"):
+        cfg["cg_presteps"] = presteps
+    return cfg
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (replicas)
+# ---------------------------------------------------------------------------
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            backend = os.environ.get("TEA_DIST_BACKEND", "gloo")
+            td.init_process_group(backend=backend)
+            self.pg = td
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v):
+        return self.reduce(v, "max")
+
+    def sum(self, v):
+        return self.reduce(v, "sum")
+
+    def reduce(self, v, op):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX if op == "max" else self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+
+class Clocks:
+    QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=5)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return float(json.load(open(path))["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel, workload):
+    """DRAM bytes per launch of the kernel from a committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        return json.load(open(path))[workload][kernel]["dram_bytes_per_launch"]
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args, dist):
+    import ctypes
+    import numpy as np
+    from tealeaf_opencl_gb300 import lib
+
+    L = lib.load()
+    name = args.workload
+    cells = WORKLOADS[name][0]
+    ncell = cells * cells
+    kernel, bytes_per_cell = WORKLOADS[name][7], WORKLOADS[name][8]
+    steps_total = args.warmup + args.steps
+    deck = deck_for(name, steps_total)
+
+    # ---- value: fields resident in HBM, fastest driver mode ----
+    drv = lib.Driver(deck, mode=lib.DRIVER_RESIDENT)
+    for _ in range(args.warmup):
+        drv.step()
+    L.tea_gb300_kernel_timer_select(kernel.encode())
+    clocks = Clocks(0)
+    dist.barrier()
+    L.tea_gb300_synchronize()
+    launches0 = L.tea_gb300_kernel_launches()
+    clocks.start()
+    t0 = time.perf_counter()
+    L.tea_gb300_event_record(0)
+    infos = [drv.step() for _ in range(args.steps)]
+    L.tea_gb300_event_record(1)
+    L.tea_gb300_synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    dist.barrier()
+    ms = float(L.tea_gb300_event_elapsed_ms(0, 1))
+    launches = L.tea_gb300_kernel_launches() - launches0
+    kms, kn = ctypes.c_double(), ctypes.c_longlong()
+    L.tea_gb300_kernel_timer_read(ctypes.byref(kms), ctypes.byref(kn))
+    L.tea_gb300_kernel_timer_select(b"")
+    drv.close()
+    outer = sum(i.iterations for i in infos)
+    inner = sum(i.inner_iterations for i in infos)
+    ms_max = dist.max(ms)
+    outer_all = dist.sum(outer)
+    value = outer_all * ncell / (ms_max / 1e3)
+
+    # ---- e2e: per-call C ABI, host buffers, copies inside the timed region ----
+    drv = lib.Driver(deck, mode=lib.DRIVER_PER_CALL)
+    for _ in range(args.warmup):
+        drv.step()
+    nbytes = ncell * 8
+    bufs = [L.tea_gb300_host_alloc(nbytes) for _ in range(3)]
+    host = [np.ctypeslib.as_array(ctypes.cast(b, ctypes.POINTER(ctypes.c_double)),
+                                  shape=(cells, cells)) for b in bufs]
+    chunk_read = lambda f, a: L.tea_gb300_read_field(lib.FIELD[f], a.ctypes.data_as(lib.PD))
+    chunk_write = lambda f, a: L.tea_gb300_write_field(lib.FIELD[f], a.ctypes.data_as(lib.PD))
+    chunk_read("density", host[0])
+    chunk_read("energy1", host[1])
+    dist.barrier()
+    L.tea_gb300_synchronize()
+    t0 = time.perf_counter()
+    e2e_outer = 0
+    for _ in range(args.steps):
+        chunk_write("density", host[0])
+        chunk_write("energy1", host[1])
+        info = drv.step()
+        chunk_read("energy1", host[2])
+        host[1][...] = host[2]
+        e2e_outer += info.iterations
+    L.tea_gb300_synchronize()
+    e2e_s = time.perf_counter() - t0
+    dist.barrier()
+    drv.close()
+    for b in bufs:
+        L.tea_gb300_host_free(b)
+    e2e_value = dist.sum(e2e_outer) * ncell / dist.max(e2e_s)
+
+    peak, peak_kind = measured_peak_hbm()
+    avg_launch_ms = kms.value / kn.value if kn.value else None
+    achieved = (bytes_per_cell * ncell / (avg_launch_ms / 1e3) / 1e9
+                if avg_launch_ms else None)
+    traffic = ncu_traffic(kernel, name)
+    out = {
+        "metric": "TeaLeaf %s cell-iterations/s at %dx%d (FP64)" % (WORKLOADS[name][1].upper(), cells, cells),
+        "value": value,
+        "unit": "cell-iters/s",
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic: five-state layout of the reference's decks",
+        "config": config_for(name),
+        "iterations": {"outer": outer, "ppcg_inner": inner,
+                       "per_step": [i.iterations for i in infos]},
+        "total_cell_iters_per_s": dist.sum(outer + inner) * ncell / (ms_max / 1e3),
+        "wall_s": wall,
+        "e2e": {"value": e2e_value, "unit": "cell-iters/s",
+                "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": nbytes,
+                "path": "per-call C ABI (host scalars), pinned host fields"},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": kernel,
+                     "achieved": achieved, "peak": peak,
+                     "peak_kind": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind
+                     if peak_kind == "measured" else "fallback",
+                     "unit": "GB/s",
+                     "frac": achieved / peak if achieved else None,
+                     "traffic": traffic,
+                     "algorithmic_bytes_per_launch": bytes_per_cell * ncell,
+                     "avg_launch_ms": avg_launch_ms, "launches_timed": kn.value},
+        "clocks": clk,
+    }
+    return out
+
+
+def cpu_sample(name, steps_timed, cap):
+    """Oracle on the same deck: one warm-up step, then steps_timed steps,
+    every step capped at `cap` outer iterations; returns (value, detail)."""
+    from oracle import oracle
+    cells = WORKLOADS[name][0]
+    deck = deck_for(name, 1 + steps_timed)
+    res = oracle.run_deck(deck, max_solver_iters=cap)
+    its = sum(res.iterations[1:1 + steps_timed])
+    secs = sum(res.step_seconds[1:1 + steps_timed])
+    return its * cells * cells / secs, {
+        "iterations": its, "seconds": secs,
+        "threads": oracle.lib().oracle_num_threads()}
+
+
+def run_reference(args, dist):
+    """The CPU restatement of the reference on the host cores."""
+    from oracle import oracle
+    name = args.workload
+    cells = WORKLOADS[name][0]
+    cap = args.cpu_cap
+    deck = deck_for(name, args.warmup + args.steps)
+    t0 = time.perf_counter()
+    res = oracle.run_deck(deck, max_solver_iters=cap)
+    wall = time.perf_counter() - t0
+    w, k = args.warmup, args.steps
+    its = sum(res.iterations[w:w + k])
+    secs = sum(res.step_seconds[w:w + k])
+    value = its * cells * cells / secs
+    threads = oracle.lib().oracle_num_threads()
+    sample = ("%d timesteps after %d warm-up steps, each capped at %d outer "
+              "iterations (%d iterations, %.1f s)" % (k, w, cap, its, secs))
+    return {
+        "impl": "reference",
+        "metric": "TeaLeaf %s cell-iterations/s at %dx%d (FP64)" % (WORKLOADS[name][1].upper(), cells, cells),
+        "value": value, "unit": "cell-iters/s", "n_gpus": dist.world,
+        "steps": k, "warmup": w, "ms_per_step": 1e3 * secs / k,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic: five-state layout of the reference's decks",
+        "config": config_for(name),
+        "cpu_baseline": {"value": value, "unit": "cell-iters/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "cell-iters/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "wall_s": wall,
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="ppcg4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-cap", type=int, default=12,
+                    help="outer iterations per CPU sample step")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
+        os.environ["CUDA_VISIBLE_DEVICES"] = os.environ.get("LOCAL_RANK", "0")
+
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        out = run_reference(args, _Solo())
+        print(json.dumps(out))
+        return
+
+    dist = Dist()
+    out = run_ours(args, dist)
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        value, detail = cpu_sample(args.workload, 1, args.cpu_cap)
+        out["cpu_baseline"] = {
+            "value": value, "unit": "cell-iters/s", "cores": detail["threads"],
+            "kind": "port",
+            "sample": "oracle (C/OpenMP restatement of the reference) on the same "
+                      "deck: step 2 after one warm-up step, capped at %d outer "
+                      "iterations (%d iterations, %.1f s)"
+                      % (args.cpu_cap, detail["iterations"], detail["seconds"])}
+    if dist.rank == 0:
+        print(json.dumps(out))
+    dist.close()
+
+
+class _Solo:
+    world = 1
+    rank = 0
+
+
+if __name__ == "__main__":
+    main()

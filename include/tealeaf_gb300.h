@@ -1,0 +1,286 @@
+/*
+ * tealeaf_gb300.h -- C ABI of the GB300 (sm_103a) TeaLeaf implicit-solve
+ * library, libtealeaf_gb300.so.
+ *
+ * Part 1 declares the entry points a TeaLeaf Fortran driver calls, with the
+ * names, argument order and by-pointer convention of UK-MAC/TeaLeaf_OpenCL
+ * (gfortran trailing underscore, implicit interfaces).  Each declaration
+ * cites the reference definition it replaces.  The library keeps one
+ * process-global chunk, as the reference does (ocl_init.cpp:9), so there is
+ * no handle.  Calls that return a scalar are synchronous; calls without an
+ * output may return before the GPU finishes (one in-order CUDA stream).
+ *
+ * Errors: by default a fatal error prints a message and aborts the process,
+ * like cloverDie (ocl_errors.cpp:175-194).  tea_gb300_set_abort_on_error(0)
+ * switches to recording the error (tea_gb300_last_error) and returning, with
+ * NaN written to any scalar output.
+ *
+ * Part 2 declares additions that have no counterpart in the reference:
+ * configuration without a tea.in file, field access, error query, and the
+ * whole-run driver.
+ */
+#ifndef TEALEAF_GB300_H
+#define TEALEAF_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------- */
+/* Part 1: reference entry points                                          */
+/* ---------------------------------------------------------------------- */
+
+/* Enumerations (kernel_files/definitions.hpp:45-56, data.f90). */
+#define TEA_PREC_NONE 1
+#define TEA_PREC_JAC_DIAG 2
+#define TEA_PREC_JAC_BLOCK 3
+#define TEA_SOLVER_JACOBI 1
+#define TEA_SOLVER_CG 2
+#define TEA_SOLVER_CHEBYSHEV 3
+#define TEA_SOLVER_PPCG 4
+#define TEA_COEF_CONDUCTIVITY 1
+#define TEA_COEF_RECIP_CONDUCTIVITY 2
+#define TEA_EXTERNAL_FACE (-1)
+/* field numbers of the fields[7] arrays (definitions.hpp:14-21) */
+#define TEA_FIELD_DENSITY 1
+#define TEA_FIELD_ENERGY0 2
+#define TEA_FIELD_ENERGY1 3
+#define TEA_FIELD_U 4
+#define TEA_FIELD_P 5
+#define TEA_FIELD_SD 6
+#define TEA_FIELD_R 7
+
+/* Replaces initialise_ocl_ (ocl_init.cpp:11-17).  Allocates the chunk of
+ * (*x_max-*x_min+1) x (*y_max-*y_min+1) cells on the current CUDA device.
+ * Halo depth, solver, preconditioner and profiler_on come from
+ * tea_gb300_configure() if it was called, else from ./tea.in with the
+ * reference's key matching (ocl_init.cpp:131-220, ocl_strings.cpp:7-37). */
+void initialise_ocl_(int* x_min, int* x_max, int* y_min, int* y_max);
+
+/* Replaces initialise_chunk_kernel_ocl_ (initialise_chunk_kernel_ocl.cpp:3-8):
+ * cell/vertex coordinates and volume (initialise_chunk_cl.cl:3-68). */
+void initialise_chunk_kernel_ocl_(double* d_xmin, double* d_ymin,
+                                  double* d_dx, double* d_dy);
+
+/* Replaces generate_chunk_kernel_ocl_ (generate_chunk_kernel_ocl.cpp:3-92):
+ * paint states (rectangle/circle/point, last wins), then u = u0 =
+ * energy0*density (generate_chunk_cl.cl:3-95). */
+void generate_chunk_kernel_ocl_(const int* number_of_states,
+                                const double* state_density,
+                                const double* state_energy,
+                                const double* state_xmin,
+                                const double* state_xmax,
+                                const double* state_ymin,
+                                const double* state_ymax,
+                                const double* state_radius,
+                                const int* state_geometry, const int* g_rect,
+                                const int* g_circ, const int* g_point);
+
+/* Replaces set_field_kernel_ocl_ (set_field_kernel_ocl.cpp:3-7):
+ * energy1 = energy0. */
+void set_field_kernel_ocl_(void);
+
+/* Replaces field_summary_kernel_ocl_ (field_summary_kernel_ocl.cpp:4-20):
+ * sums of volume, mass, mass*energy1 and mass*u over the interior. */
+void field_summary_kernel_ocl_(double* vol, double* mass, double* ie,
+                               double* temp);
+
+/* Replaces update_halo_kernel_ocl_ (update_halo_kernel_ocl.cpp:6-62):
+ * reflective halo update of density, energy0, energy1 (fields[0..2] == 1)
+ * to the given depth on every external face, as one fused launch. */
+void update_halo_kernel_ocl_(const int* chunk_neighbours, const int* fields,
+                             const int* depth);
+
+/* Replaces tea_leaf_common_init_kernel_ocl_ (tea_leaf_kernel_ocl.cpp:233-239,
+ * :254-289): rx = dt/dx^2, ry = dt/dy^2; face coefficients Kx, Ky; boundary
+ * faces zeroed unless *reflective_boundary; u = u0 = energy1*density. */
+void tea_leaf_common_init_kernel_ocl_(const int* coefficient, double* dt,
+                                      double* rx, double* ry,
+                                      int* zero_boundary,
+                                      int* reflective_boundary);
+
+/* Replaces tea_leaf_calc_residual_ocl_ (tea_leaf_kernel_ocl.cpp:248-252):
+ * r = u0 - A u. */
+void tea_leaf_calc_residual_ocl_(void);
+
+/* Replaces tea_leaf_calc_2norm_kernel_ocl_ (tea_leaf_kernel_ocl.cpp:34-38,
+ * :56-96): *norm_array 0 -> u0.u0, 1 -> r.r, 2 -> r.z (r.r without a
+ * preconditioner). */
+void tea_leaf_calc_2norm_kernel_ocl_(int* norm_array, double* norm);
+
+/* Replaces tea_leaf_cg_init_kernel_ocl_ (tea_leaf_kernel_ocl.cpp:143-147,
+ * :167-187): build the preconditioner, z = M^-1 r, p = z, *rro = r.p. */
+void tea_leaf_cg_init_kernel_ocl_(double* rro);
+
+/* Replaces tea_leaf_cg_calc_w_kernel_ocl_ (tea_leaf_kernel_ocl.cpp:149-153,
+ * :189-194): w = A p, *pw = p.w. */
+void tea_leaf_cg_calc_w_kernel_ocl_(double* pw);
+
+/* Replaces tea_leaf_cg_calc_ur_kernel_ocl_ (tea_leaf_kernel_ocl.cpp:154-158,
+ * :196-204): u += alpha p, r -= alpha w, z = M^-1 r, *rrn = r.z. */
+void tea_leaf_cg_calc_ur_kernel_ocl_(double* alpha, double* rrn);
+
+/* Replaces tea_leaf_cg_calc_p_kernel_ocl_ (tea_leaf_kernel_ocl.cpp:159-163,
+ * :206-212): p = z + beta p. */
+void tea_leaf_cg_calc_p_kernel_ocl_(double* beta);
+
+/* Replaces tea_leaf_cheby_init_kernel_ocl_ (tea_leaf_kernel_ocl.cpp:42-48,
+ * :98-129): keep *n_coefs Chebyshev coefficients, then w = A u,
+ * r = u0 - w, p = M^-1 r / theta, u += p.  No size limit applies (the
+ * reference is bounded by the device's constant-buffer size). */
+void tea_leaf_cheby_init_kernel_ocl_(const double* ch_alphas,
+                                     const double* ch_betas, int* n_coefs,
+                                     const double* rx, const double* ry,
+                                     const double* theta);
+
+/* Replaces tea_leaf_cheby_iterate_kernel_ocl_ (tea_leaf_kernel_ocl.cpp:50-54,
+ * :131-138): w = A u, r = u0 - w, p = alpha[s] p + beta[s] M^-1 r, u += p
+ * with s = *cheby_calc_step - 1. */
+void tea_leaf_cheby_iterate_kernel_ocl_(const int* cheby_calc_step);
+
+/* Replaces tea_leaf_ppcg_init_ocl_ (tea_leaf_kernel_ocl.cpp:306-311,
+ * :327-344): keep *n_inner_steps coefficients and theta. */
+void tea_leaf_ppcg_init_ocl_(const double* ch_alphas, const double* ch_betas,
+                             double* theta, int* n_inner_steps);
+
+/* Replaces tea_leaf_ppcg_init_sd_kernel_ocl_ (tea_leaf_kernel_ocl.cpp:313-317,
+ * :346-350): sd = M^-1 r / theta. */
+void tea_leaf_ppcg_init_sd_kernel_ocl_(void);
+
+/* Replaces tea_leaf_ppcg_inner_kernel_ocl_ (tea_leaf_kernel_ocl.cpp:319-325,
+ * :352-411): u += sd, r -= A sd, sd = alpha[s] sd + beta[s] M^-1 r with
+ * s = *inner_step - 1.  Single chunk: every neighbour must be
+ * TEA_EXTERNAL_FACE, so *bounds_extra does not change the range. */
+void tea_leaf_ppcg_inner_kernel_ocl_(int* inner_step, int* bounds_extra,
+                                     const int* chunk_neighbours);
+
+/* Replaces tea_leaf_jacobi_solve_kernel_ocl_ (tea_leaf_kernel_ocl.cpp:216-229):
+ * un = u, one Jacobi sweep, *error = sum |u - un|. */
+void tea_leaf_jacobi_solve_kernel_ocl_(double* error);
+
+/* Replaces tea_leaf_common_finalise_kernel_ocl_
+ * (tea_leaf_kernel_ocl.cpp:242-246, :292-296): energy1 = u / density. */
+void tea_leaf_common_finalise_kernel_ocl_(void);
+
+/* Replaces print_opencl_profiling_info_ (ocl_errors.cpp:196-232): per-kernel
+ * call counts and times, collected when profiler_on is set. */
+void print_opencl_profiling_info_(void);
+
+/* Replace ocl_pack_buffers_ / ocl_unpack_buffers_ (ocl_pack.cpp:4-16).  MPI
+ * halo exchange is out of scope for a single chunk: these accept only calls
+ * that exchange no field and report an error otherwise. */
+void ocl_pack_buffers_(int* fields, int* offsets, int* depth, int* face,
+                       double* host_buffer);
+void ocl_unpack_buffers_(int* fields, int* offsets, int* depth, int* face,
+                         double* host_buffer);
+
+/* ---------------------------------------------------------------------- */
+/* Part 2: additions (no counterpart in the reference)                     */
+/* ---------------------------------------------------------------------- */
+
+/* Field numbers for tea_gb300_read_field / write_field: 1..7 as above, and */
+#define TEA_FIELD_U0 8
+#define TEA_FIELD_W 9
+#define TEA_FIELD_Z 10
+#define TEA_FIELD_MI 11
+#define TEA_FIELD_KX 12
+#define TEA_FIELD_KY 13
+#define TEA_FIELD_CP 14
+#define TEA_FIELD_BFP 15
+#define TEA_FIELD_VOLUME 16
+
+/* Sets what initialise_ocl_ would otherwise read from ./tea.in.  Returns 0,
+ * or -1 for invalid values. */
+int tea_gb300_configure(int halo_depth, int solver, int preconditioner,
+                        int profiler_on);
+
+/* 1 (default): fatal errors abort; 0: record and return. */
+void tea_gb300_set_abort_on_error(int abort_on_error);
+
+/* 0 if no error was recorded since the last call, else the error code; the
+ * message is copied to msg (may be NULL).  Clears the recorded error. */
+int tea_gb300_last_error(char* msg, int msg_len);
+
+/* Frees the chunk's device memory. */
+void tea_gb300_finalise(void);
+
+/* Interior of a field (x fastest, y_max rows of x_max), host <-> device,
+ * synchronous.  Return 0 or -1. */
+int tea_gb300_read_field(int field, double* out);
+int tea_gb300_write_field(int field, const double* in);
+/* The padded field ((x_max+2H) x (y_max+2H), x fastest), as the reference
+ * lays it out. */
+int tea_gb300_read_field_padded(int field, double* out);
+int tea_gb300_write_field_padded(int field, const double* in);
+
+/* Rows per reduction tile for a grid (4 or 16); the summation order is
+ * documented with the kernels. */
+int tea_gb300_reduction_rows(int x_max, int y_max);
+
+/* Number of kernel launches this library has made since load. */
+long long tea_gb300_kernel_launches(void);
+
+/* The cudaStream_t all work is queued on. */
+void* tea_gb300_stream(void);
+
+/* Chunk geometry: x_max, y_max, halo depth, row stride in doubles. */
+int tea_gb300_chunk_info(int* x_max, int* y_max, int* halo, int* stride);
+
+/* Timing on the library's stream: record CUDA event `slot` (0..15) now;
+ * elapsed milliseconds between two recorded slots (waits for the second). */
+int tea_gb300_event_record(int slot);
+float tea_gb300_event_elapsed_ms(int start_slot, int end_slot);
+
+/* Times every launch of the kernel with the given name (as listed by
+ * print_opencl_profiling_info_) with CUDA events on the library's stream,
+ * without serialising other work.  Selecting resets the totals; NULL or ""
+ * stops timing.  Read returns the summed milliseconds and launch count. */
+int tea_gb300_kernel_timer_select(const char* name);
+int tea_gb300_kernel_timer_read(double* total_ms, long long* launches);
+
+/* Waits for all work queued on the library's stream. */
+int tea_gb300_synchronize(void);
+
+/* Page-locked host memory for fast field copies. */
+void* tea_gb300_host_alloc(size_t bytes);
+void tea_gb300_host_free(void* p);
+
+/* ---- whole-run driver (C++ restatement of the Fortran driver) ---- */
+
+/* Solve-loop implementations the driver can use. */
+#define TEA_DRIVER_PER_CALL 0  /* reference call sequence, host scalars */
+#define TEA_DRIVER_RESIDENT 1  /* CG iterations kept on the device */
+
+typedef struct {
+  int step;               /* timestep number */
+  double time;            /* simulated time after the step */
+  double dt;
+  int iterations;         /* solver loop iterations run in this step */
+  int inner_iterations;   /* PPCG inner steps run in this step */
+  double conduction_error; /* final error / initial residual */
+  double exact_error;     /* tl_check_result residual (NaN if not asked) */
+  int summary_done;       /* 1 if a field summary ran in this step */
+  double vol, mass, ie, temp; /* that field summary */
+  int complete;           /* 1 after the last step of the deck */
+  int qa_passed;          /* test problem check: 1, 0, or -1 (none) */
+  double qa_diff;
+} tea_gb300_step_info;
+
+/* Parses a tea.in deck (its text), sets up the problem on the GPU (as
+ * start.f90 does, including the first field summary).  log_path may be
+ * NULL, else a tea.out-style log is written.  max_iters_cap > 0 limits
+ * solver iterations per step.  Returns 0 or -1 (see tea_gb300_last_error). */
+int tea_gb300_driver_open(const char* deck_text, const char* log_path,
+                          int mode, int max_iters_cap);
+/* One timestep (timestep, tea_leaf, summaries).  Returns 0, 1 when the deck
+ * had already completed, or -1 on error. */
+int tea_gb300_driver_step(tea_gb300_step_info* info);
+/* Closes the log; the chunk stays allocated for inspection. */
+void tea_gb300_driver_close(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,882 @@
+/*
+ * TEST INFRASTRUCTURE ONLY -- CPU oracle, kernel half.
+ *
+ * One C function per OpenCL kernel of UK-MAC/TeaLeaf_OpenCL that the implicit
+ * solve runs, with the kernel's arithmetic written in the kernel's own
+ * operation order and over the kernel's own launch range.  Launch ranges come
+ * from the KERNEL_{X,Y}_{MIN,MAX} bounds given to compileKernel
+ * (ocl_kernels.cpp:51-114) combined with findPaddingSize
+ * (ocl_kernels.cpp:123-134) and WITHIN_BOUNDS (macros_cl.cl:25-29):
+ *   bounds (0,0)   -> interior  col in [H, H+x_max), row in [H, H+y_max)
+ *   bounds (1-H,H) -> col in [1, x_max+2H), row in [1, y_max+2H)
+ *   bounds (-H,H)  -> the whole padded array
+ * Fields use the reference layout: element (col,row) at col + row*(x_max+2H)
+ * (THARR2D, macros_cl.cl:20-22), each array holding (x_max+2H+1)*(y_max+2H+1)
+ * zero-initialised doubles (ocl_buffers.cpp:6-69).
+ *
+ * Build with -ffp-contract=off: no multiply-add contraction, so every result
+ * is the IEEE double result of the expression as written.
+ */
+#include "tea_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef struct {
+  int x_max, y_max, H, solver, prec;
+  int xs, ys;
+  long n2;
+  double *density, *energy0, *energy1, *volume;
+  double *cellx, *celldx, *vertexx, *vertexdx;
+  double *celly, *celldy, *vertexy, *vertexdy;
+  double *p, *r, *w, *Mi, *Kx, *Ky, *sd, *u, *u0, *z, *cp, *bfp;
+  double *ch_alphas, *ch_betas;
+  double *ztmp; /* M^-1 r kept out of z where the reference keeps it local */
+  int n_coefs;
+  double theta_cheby, theta_ppcg;
+  double *scratch[4];
+} OrcChunk;
+
+static OrcChunk C;
+static int C_ready = 0;
+
+#define IDX(col, row) ((long)(col) + (long)(row) * C.xs)
+
+/* ------------------------------------------------------------------------ */
+/* Canonical fixed-order summation                                          */
+/* ------------------------------------------------------------------------ */
+/*
+ * Interior cells (x in [0,x_max), y in [0,y_max)) are cut into tiles of 32
+ * columns x TH rows, and tiles into supertiles of 8 tiles along x
+ * (256 columns x TH rows).
+ *   1. lane l of a tile holds column 32*tx+l; it adds its TH rows bottom to
+ *      top into an accumulator that starts at +0.0 (cells outside the
+ *      interior add +0.0);
+ *   2. the 32 lane sums are combined by a butterfly: for offset 16,8,4,2,1
+ *      every lane l replaces a[l] by a[l] + a[l^offset]; the tile sum is a[0];
+ *   3. a supertile sum is the same butterfly over 32 lanes whose first 8
+ *      hold the tile sums (0.0 for tiles past the interior), the rest 0.0;
+ *   4. supertile sums are numbered row-major (sy*nsx+sx); lane i of 256
+ *      adds sums i, i+256, i+512, ... in order from +0.0; each group of 32
+ *      lanes is butterflied, and the 8 group sums are butterflied as in 3.
+ * TH is 16 when the grid has at least 1216 supertiles of 16 rows, else 4.
+ */
+int oracle_reduction_rows(int x_max, int y_max) {
+  long nsx = (x_max + 255) / 256;
+  long nsy16 = (y_max + 15) / 16;
+  return (nsx * nsy16 >= 1216) ? 16 : 4;
+}
+
+static double butterfly32(const double* v) {
+  double a[32], b[32];
+  memcpy(a, v, sizeof(a));
+  for (int off = 16; off >= 1; off >>= 1) {
+    for (int l = 0; l < 32; l++) b[l] = a[l] + a[l ^ off];
+    memcpy(a, b, sizeof(a));
+  }
+  return a[0];
+}
+
+static double sum8(const double* v8) {
+  double a[32];
+  for (int l = 0; l < 32; l++) a[l] = (l < 8) ? v8[l] : 0.0;
+  return butterfly32(a);
+}
+
+double oracle_reduce(const double* contrib, int X, int Y) {
+  const int TH = oracle_reduction_rows(X, Y);
+  const long ntx = (X + 31) / 32;
+  const long nty = (Y + TH - 1) / TH;
+  const long nsx = (ntx + 7) / 8;
+  const long ns = nsx * nty;
+  double* S = (double*)malloc(sizeof(double) * (size_t)(ns > 0 ? ns : 1));
+#pragma omp parallel for schedule(static)
+  for (long s = 0; s < ns; s++) {
+    const long sy = s / nsx, sx = s % nsx;
+    double t8[8];
+    for (int wv = 0; wv < 8; wv++) {
+      const long tx = 8 * sx + wv;
+      if (tx >= ntx) {
+        t8[wv] = 0.0;
+        continue;
+      }
+      double lanes[32];
+      for (int l = 0; l < 32; l++) {
+        const long col = 32 * tx + l;
+        double acc = 0.0;
+        for (int j = 0; j < TH; j++) {
+          const long row = (long)TH * sy + j;
+          const double v = (col < X && row < Y) ? contrib[row * X + col] : 0.0;
+          acc = acc + v;
+        }
+        lanes[l] = acc;
+      }
+      t8[wv] = butterfly32(lanes);
+    }
+    S[s] = sum8(t8);
+  }
+  double lanes256[256];
+  for (int i = 0; i < 256; i++) {
+    double acc = 0.0;
+    for (long k = i; k < ns; k += 256) acc = acc + S[k];
+    lanes256[i] = acc;
+  }
+  double w8[8];
+  for (int wv = 0; wv < 8; wv++) w8[wv] = butterfly32(lanes256 + 32 * wv);
+  free(S);
+  return sum8(w8);
+}
+
+/* sum of an interior-indexed scratch array */
+static double reduce_scratch(int k) {
+  return oracle_reduce(C.scratch[k], C.x_max, C.y_max);
+}
+
+#define SCR(k, col, row) \
+  C.scratch[k][(long)((row)-C.H) * C.x_max + ((col)-C.H)]
+
+/* ------------------------------------------------------------------------ */
+/* Lifecycle                                                                */
+/* ------------------------------------------------------------------------ */
+
+static double* zalloc(long n) {
+  double* p = (double*)calloc((size_t)n, sizeof(double));
+  return p;
+}
+
+void oracle_finalise(void) {
+  if (!C_ready) return;
+  double** all[] = {&C.density, &C.energy0, &C.energy1, &C.volume, &C.cellx,
+                    &C.celldx,  &C.vertexx, &C.vertexdx, &C.celly, &C.celldy,
+                    &C.vertexy, &C.vertexdy, &C.p, &C.r, &C.w, &C.Mi, &C.Kx,
+                    &C.Ky, &C.sd, &C.u, &C.u0, &C.z, &C.cp, &C.bfp,
+                    &C.ch_alphas, &C.ch_betas, &C.ztmp, &C.scratch[0], &C.scratch[1],
+                    &C.scratch[2], &C.scratch[3]};
+  for (size_t i = 0; i < sizeof(all) / sizeof(all[0]); i++) {
+    free(*all[i]);
+    *all[i] = NULL;
+  }
+  C_ready = 0;
+}
+
+/* initialise_ocl_ (ocl_init.cpp:11-17) + initBuffers (ocl_buffers.cpp). */
+int oracle_initialise(int x_max, int y_max, int H, int solver, int prec) {
+  oracle_finalise();
+  if (x_max < 1 || y_max < 1 || H < 1) return -1;
+  memset(&C, 0, sizeof(C));
+  C.x_max = x_max;
+  C.y_max = y_max;
+  C.H = H;
+  C.solver = solver;
+  C.prec = prec;
+  C.xs = x_max + 2 * H;
+  C.ys = y_max + 2 * H;
+  C.n2 = (long)(C.xs + 1) * (C.ys + 1);
+  double** f2[] = {&C.density, &C.energy0, &C.energy1, &C.volume, &C.p, &C.r,
+                   &C.w,       &C.Mi,      &C.Kx,      &C.Ky,     &C.sd, &C.u,
+                   &C.u0,      &C.z,       &C.cp,      &C.bfp,    &C.ztmp};
+  for (size_t i = 0; i < sizeof(f2) / sizeof(f2[0]); i++) {
+    *f2[i] = zalloc(C.n2);
+    if (!*f2[i]) return -2;
+  }
+  double** f1[] = {&C.cellx, &C.celldx, &C.vertexx, &C.vertexdx,
+                   &C.celly, &C.celldy, &C.vertexy, &C.vertexdy};
+  for (size_t i = 0; i < sizeof(f1) / sizeof(f1[0]); i++) {
+    *f1[i] = zalloc((C.xs > C.ys ? C.xs : C.ys) + 2);
+    if (!*f1[i]) return -2;
+  }
+  for (int k = 0; k < 4; k++) {
+    C.scratch[k] = zalloc((long)x_max * y_max);
+    if (!C.scratch[k]) return -2;
+  }
+  C_ready = 1;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Setup kernels                                                            */
+/* ------------------------------------------------------------------------ */
+
+/* initialise_chunk_first / _second, initialise_chunk_cl.cl:3-68.  xarea and
+ * yarea are not computed: no kernel of the solve or field summary reads
+ * them. */
+void oracle_initialise_chunk(double xmin, double ymin, double dx, double dy) {
+  const int H = C.H;
+  for (int col = 0; col <= C.x_max + H; col++) {
+    C.vertexx[col] = xmin + dx * (double)(((col)-1) - H + 1);
+    C.vertexdx[col] = dx;
+    const double plus1 = xmin + dx * (double)((col)-H + 1);
+    C.cellx[col] = 0.5 * (C.vertexx[col] + plus1);
+    C.celldx[col] = dx;
+  }
+  for (int row = 0; row <= C.y_max + H; row++) {
+    C.vertexy[row] = ymin + dy * (double)(((row)-1) - H + 1);
+    C.vertexdy[row] = dy;
+    const double plus1 = ymin + dy * (double)((row)-H + 1);
+    C.celly[row] = 0.5 * (C.vertexy[row] + plus1);
+    C.celldy[row] = dy;
+  }
+  for (int row = H - 1; row <= C.y_max + H; row++)
+    for (int col = H - 1; col <= C.x_max + H; col++)
+      C.volume[IDX(col, row)] = dx * dy;
+}
+
+/* generate_chunk_init, generate_chunk, generate_chunk_init_u
+ * (generate_chunk_cl.cl:3-95), in the order of
+ * generate_chunk_kernel_ocl.cpp:52-91.  Geometry codes: 1 rectangle,
+ * 2 circle, 3 point (data.f90 g_rect/g_circ/g_point). */
+void oracle_generate_chunk(int nstates, const double* sd, const double* se,
+                           const double* sxmin, const double* sxmax,
+                           const double* symin, const double* symax,
+                           const double* sradius, const int* sgeom) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++) {
+    for (int col = H; col < H + C.x_max; col++) {
+      C.energy0[IDX(col, row)] = se[0];
+      C.density[IDX(col, row)] = sd[0];
+    }
+  }
+  for (int s = 1; s < nstates; s++) {
+#pragma omp parallel for schedule(static)
+    for (int row = H; row < H + C.y_max; row++) {
+      for (int col = H; col < H + C.x_max; col++) {
+        const double x_cent = sxmin[s];
+        const double y_cent = symin[s];
+        int hit = 0;
+        if (sgeom[s] == 1) {
+          hit = C.vertexx[1 + col] >= sxmin[s] && C.vertexx[col] < sxmax[s] &&
+                C.vertexy[1 + row] >= symin[s] && C.vertexy[row] < symax[s];
+        } else if (sgeom[s] == 2) {
+          const double x_pos = C.cellx[col] - x_cent;
+          const double y_pos = C.celly[row] - y_cent;
+          const double radius = sqrt(x_pos * x_pos + y_pos * y_pos);
+          hit = radius <= sradius[s];
+        } else if (sgeom[s] == 3) {
+          hit = C.vertexx[col] == x_cent && C.vertexy[row] == y_cent;
+        }
+        if (hit) {
+          C.energy0[IDX(col, row)] = se[s];
+          C.density[IDX(col, row)] = sd[s];
+        }
+      }
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++) {
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      C.u[c] = C.energy0[c] * C.density[c];
+      C.u0[c] = C.energy0[c] * C.density[c];
+    }
+  }
+}
+
+/* set_field_cl.cl:3-13 */
+void oracle_set_field(void) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++)
+      C.energy1[IDX(col, row)] = C.energy0[IDX(col, row)];
+}
+
+/* ------------------------------------------------------------------------ */
+/* Solver kernels                                                           */
+/* ------------------------------------------------------------------------ */
+
+/* The 5-point operator exactly as written inline in every kernel, e.g.
+ * tea_leaf_cg_cl.cl:59-63. */
+static inline double smvp_at(const double* x, long c) {
+  const long xs = C.xs;
+  return (1.0 + (C.Ky[c + xs] + C.Ky[c]) + (C.Kx[c + 1] + C.Kx[c])) * x[c] -
+         (C.Ky[c + xs] * x[c + xs] + C.Ky[c] * x[c - xs]) -
+         (C.Kx[c + 1] * x[c + 1] + C.Kx[c] * x[c - 1]);
+}
+
+/* Rows in the 4-row block-Jacobi strip starting at interior row 4g:
+ * BLOCK_TOP, macros_cl.cl:6-10, enabled when y_max % 4 != 0
+ * (ocl_kernels.cpp:26-29).  The reference's formula min(y_max+2-row, 4)
+ * (row = H+4g) counts one halo row too many when H = 1 and is exact when
+ * H = 2; for H >= 3 it undercounts and reads unset local memory, so there the
+ * strip is taken as the remaining interior rows. */
+static inline int block_top(int g) {
+  if (C.y_max % 4 == 0) return 4;
+  int up = C.y_max - 4 * g + (C.H == 1 ? 1 : 0);
+  return up < 4 ? up : 4;
+}
+
+#define COEF_A(rk) (-C.Ky[IDX(col, rk)])
+#define COEF_B(rk)                                                 \
+  (1.0 + (C.Ky[IDX(col, (rk) + 1)] + C.Ky[IDX(col, rk)]) +         \
+   (C.Kx[IDX(col + 1, rk)] + C.Kx[IDX(col, rk)]))
+#define COEF_C(rk) (-C.Ky[IDX(col, (rk) + 1)])
+
+/* tea_leaf_block_init, tea_block_jacobi.cl:78-105 */
+static void block_init(void) {
+  const int H = C.H;
+  const int ng = (C.y_max + 3) / 4;
+#pragma omp parallel for schedule(static)
+  for (int g = 0; g < ng; g++) {
+    const int row0 = H + 4 * g;
+    const int upper = block_top(g);
+    for (int col = H; col < H + C.x_max; col++) {
+      C.cp[IDX(col, row0)] = COEF_C(row0) / COEF_B(row0);
+      for (int k = 1; k < upper; k++) {
+        const int rk = row0 + k;
+        C.bfp[IDX(col, rk)] =
+            1.0 / (COEF_B(rk) - COEF_A(rk) * C.cp[IDX(col, rk - 1)]);
+        C.cp[IDX(col, rk)] = COEF_C(rk) * C.bfp[IDX(col, rk)];
+      }
+    }
+  }
+}
+
+/* block_solve_func, tea_block_jacobi.cl:6-42, applied to every strip:
+ * zout = M_block^-1 rin.  Rows of the strip beyond the interior read r = 0
+ * (the kernels zero their local copy there); z is written on interior rows
+ * only. */
+static void block_solve(const double* rin, double* zout) {
+  const int H = C.H;
+  const int ng = (C.y_max + 3) / 4;
+#pragma omp parallel for schedule(static)
+  for (int g = 0; g < ng; g++) {
+    const int row0 = H + 4 * g;
+    const int upper = block_top(g);
+    for (int col = H; col < H + C.x_max; col++) {
+      double rl[4], dp[4], zl[4];
+      for (int k = 0; k < 4; k++) {
+        const int rk = row0 + k;
+        rl[k] = (rk < H + C.y_max) ? rin[IDX(col, rk)] : 0.0;
+      }
+      dp[0] = rl[0] / COEF_B(row0);
+      for (int k = 1; k < upper; k++) {
+        const int rk = row0 + k;
+        dp[k] = (rl[k] - COEF_A(rk) * dp[k - 1]) * C.bfp[IDX(col, rk)];
+      }
+      zl[upper - 1] = dp[upper - 1];
+      for (int k = upper - 2; k >= 0; k--)
+        zl[k] = dp[k] - C.cp[IDX(col, row0 + k)] * zl[k + 1];
+      for (int k = 0; k < upper; k++) {
+        const int rk = row0 + k;
+        if (rk < H + C.y_max) zout[IDX(col, rk)] = zl[k];
+      }
+    }
+  }
+}
+
+/* tea_leaf_init_common + tea_leaf_zero_boundary + generate_chunk_init_u with
+ * energy1, as run by CloverChunk::tea_leaf_common_init
+ * (tea_leaf_kernel_ocl.cpp:254-289); rx, ry from calcrxry (:8-32), which
+ * reads celldx/celldy at index H+1. */
+void oracle_common_init(int coef, double dt, double* rx, double* ry,
+                        const int* zero_boundary, int reflective) {
+  const int H = C.H;
+  const double dx = C.celldx[1 + H];
+  const double dy = C.celldy[1 + H];
+  const double RX = dt / (dx * dx);
+  const double RY = dt / (dy * dy);
+  *rx = RX;
+  *ry = RY;
+  /* tea_leaf_common_cl.cl:56-90 over [1, x_max+2H) x [1, y_max+2H) */
+#pragma omp parallel for schedule(static)
+  for (int row = 1; row < C.ys; row++) {
+    for (int col = 1; col < C.xs; col++) {
+      const long c = IDX(col, row);
+      double dc = 0.0, dl = 0.0, dd = 0.0;
+      if (coef == ORC_COEF_CONDUCTIVITY) {
+        dc = C.density[c];
+        dl = C.density[c - 1];
+        dd = C.density[c - C.xs];
+      } else if (coef == ORC_COEF_RECIP_CONDUCTIVITY) {
+        dc = 1.0 / C.density[c];
+        dl = 1.0 / C.density[c - 1];
+        dd = 1.0 / C.density[c - C.xs];
+      }
+      double kx = (dl + dc) / (2.0 * dl * dc);
+      kx = kx * RX;
+      double ky = (dd + dc) / (2.0 * dd * dc);
+      ky = ky * RY;
+      C.Kx[c] = kx;
+      C.Ky[c] = ky;
+    }
+  }
+  if (!reflective) {
+    /* tea_leaf_common_cl.cl:92-125 over the whole padded array */
+    const int zl = zero_boundary[0], zr = zero_boundary[1];
+    const int zb = zero_boundary[2], zt = zero_boundary[3];
+#pragma omp parallel for schedule(static)
+    for (int row = 0; row < C.ys; row++) {
+      for (int col = 0; col < C.xs; col++) {
+        const long c = IDX(col, row);
+        if (zl && col <= H) {
+          C.Kx[c] = 0;
+          if (col < H) C.Ky[c] = 0;
+        }
+        if (zr && col > (C.x_max - 1) + H) {
+          C.Kx[c] = 0;
+          C.Ky[c] = 0;
+        }
+        if (zb && row <= H) {
+          C.Ky[c] = 0;
+          if (row < H) C.Kx[c] = 0;
+        }
+        if (zt && row > (C.y_max - 1) + H) {
+          C.Ky[c] = 0;
+          C.Kx[c] = 0;
+        }
+      }
+    }
+  }
+  /* generate_chunk_cl.cl:67-80 with energy1 */
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++) {
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      C.u[c] = C.energy1[c] * C.density[c];
+      C.u0[c] = C.energy1[c] * C.density[c];
+    }
+  }
+}
+
+/* tea_leaf_calc_residual, tea_leaf_common_cl.cl:17-36 */
+void oracle_calc_residual(void) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      const double smvp = smvp_at(C.u, c);
+      C.r[c] = C.u0[c] - smvp;
+    }
+}
+
+/* tea_leaf_calc_2norm, tea_leaf_common_cl.cl:38-54, with the argument
+ * binding of tea_leaf_kernel_ocl.cpp:56-96 */
+void oracle_calc_2norm(int which, double* norm) {
+  const double *a, *b;
+  if (which == 0) {
+    a = C.u0;
+    b = C.u0;
+  } else if (which == 1) {
+    a = C.r;
+    b = C.r;
+  } else if (which == 2) {
+    a = C.r;
+    b = (C.prec == ORC_PREC_NONE) ? C.r : C.z;
+  } else {
+    *norm = NAN;
+    return;
+  }
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      SCR(0, col, row) = a[c] * b[c];
+    }
+  *norm = reduce_scratch(0);
+}
+
+/* tea_leaf_init_jac_diag, tea_leaf_common_cl.cl:127-142, whole array */
+static void init_jac_diag(void) {
+#pragma omp parallel for schedule(static)
+  for (int row = 0; row < C.ys; row++)
+    for (int col = 0; col < C.xs; col++) {
+      const long c = IDX(col, row);
+      const double diag =
+          (1.0 + (C.Ky[c + C.xs] + C.Ky[c]) + (C.Kx[c + 1] + C.Kx[c]));
+      C.Mi[c] = 1.0 / diag;
+    }
+}
+
+/* CloverChunk::tea_leaf_cg_init_kernel, tea_leaf_kernel_ocl.cpp:167-187;
+ * tea_leaf_cg_solve_init_p, tea_leaf_cg_cl.cl:8-41 */
+void oracle_cg_init(double* rro) {
+  const int H = C.H;
+  if (C.prec == ORC_PREC_JAC_BLOCK) {
+    block_init();
+    block_solve(C.r, C.z);
+  } else if (C.prec == ORC_PREC_JAC_DIAG) {
+    init_jac_diag();
+  }
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      if (C.prec == ORC_PREC_JAC_BLOCK) {
+        C.p[c] = C.z[c];
+      } else if (C.prec == ORC_PREC_JAC_DIAG) {
+        C.z[c] = C.r[c] * C.Mi[c];
+        C.p[c] = C.z[c];
+      } else {
+        C.p[c] = C.r[c];
+      }
+      SCR(0, col, row) = C.r[c] * C.p[c];
+    }
+  *rro = reduce_scratch(0);
+}
+
+/* tea_leaf_cg_solve_calc_w, tea_leaf_cg_cl.cl:45-69 */
+void oracle_cg_calc_w(double* pw) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      C.w[c] = smvp_at(C.p, c);
+      SCR(0, col, row) = C.p[c] * C.w[c];
+    }
+  *pw = reduce_scratch(0);
+}
+
+/* tea_leaf_cg_solve_calc_ur, tea_leaf_cg_cl.cl:73-137 */
+void oracle_cg_calc_ur(double alpha, double* rrn) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      C.u[c] = C.u[c] + alpha * C.p[c];
+      C.r[c] = C.r[c] - alpha * C.w[c];
+    }
+  if (C.prec == ORC_PREC_JAC_BLOCK) block_solve(C.r, C.z);
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      if (C.prec == ORC_PREC_JAC_BLOCK) {
+        SCR(0, col, row) = C.r[c] * C.z[c];
+      } else if (C.prec == ORC_PREC_JAC_DIAG) {
+        C.z[c] = C.r[c] * C.Mi[c];
+        SCR(0, col, row) = C.r[c] * C.z[c];
+      } else {
+        SCR(0, col, row) = C.r[c] * C.r[c];
+      }
+    }
+  *rrn = reduce_scratch(0);
+}
+
+/* tea_leaf_cg_solve_calc_p, tea_leaf_cg_cl.cl:141-160 */
+void oracle_cg_calc_p(double beta) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      if (C.prec != ORC_PREC_NONE)
+        C.p[c] = C.z[c] + beta * C.p[c];
+      else
+        C.p[c] = C.r[c] + beta * C.p[c];
+    }
+}
+
+static void store_coefs(const double* a, const double* b, int n) {
+  free(C.ch_alphas);
+  free(C.ch_betas);
+  C.ch_alphas = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+  C.ch_betas = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+  if (n > 0) {
+    memcpy(C.ch_alphas, a, sizeof(double) * (size_t)n);
+    memcpy(C.ch_betas, b, sizeof(double) * (size_t)n);
+  }
+  C.n_coefs = n;
+}
+
+/* w = A u; r = u0 - w (first half of tea_leaf_cheby_solve_init_p and
+ * tea_leaf_cheby_solve_calc_p, tea_leaf_cheby_cl.cl:14-26, :88-100) */
+static void cheby_residual(void) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      C.w[c] = smvp_at(C.u, c);
+      C.r[c] = C.u0[c] - C.w[c];
+    }
+}
+
+/* tea_leaf_cheby_solve_calc_u, tea_leaf_cheby_cl.cl:66-76 */
+static void cheby_calc_u(void) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      C.u[c] = C.u[c] + C.p[c];
+    }
+}
+
+/* CloverChunk::tea_leaf_cheby_init_kernel, tea_leaf_kernel_ocl.cpp:98-129:
+ * store coefficients, run cheby_solve_init_p then cheby_solve_calc_u. */
+void oracle_cheby_init(const double* alphas, const double* betas, int n,
+                       double theta) {
+  const int H = C.H;
+  store_coefs(alphas, betas, n);
+  C.theta_cheby = theta;
+  cheby_residual();
+  if (C.prec == ORC_PREC_JAC_BLOCK) block_solve(C.r, C.ztmp);
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      if (C.prec == ORC_PREC_JAC_BLOCK)
+        C.p[c] = C.ztmp[c] / theta;
+      else if (C.prec == ORC_PREC_JAC_DIAG)
+        C.p[c] = (C.Mi[c] * C.r[c]) / theta;
+      else
+        C.p[c] = C.r[c] / theta;
+    }
+  cheby_calc_u();
+}
+
+/* CloverChunk::tea_leaf_cheby_iterate_kernel (tea_leaf_kernel_ocl.cpp:131-138):
+ * cheby_solve_calc_p (tea_leaf_cheby_cl.cl:78-145) with coefficient index
+ * step-1, then cheby_solve_calc_u.  In the block-Jacobi case the reference
+ * keeps M^-1 r in local memory only and leaves z untouched. */
+void oracle_cheby_iterate(int step) {
+  const int H = C.H;
+  const int s = step - 1;
+  const double a = C.ch_alphas[s], b = C.ch_betas[s];
+  cheby_residual();
+  if (C.prec == ORC_PREC_JAC_BLOCK) block_solve(C.r, C.ztmp);
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      if (C.prec == ORC_PREC_JAC_BLOCK)
+        C.p[c] = a * C.p[c] + b * C.ztmp[c];
+      else if (C.prec == ORC_PREC_JAC_DIAG)
+        C.p[c] = a * C.p[c] + b * C.Mi[c] * C.r[c];
+      else
+        C.p[c] = a * C.p[c] + b * C.r[c];
+    }
+  cheby_calc_u();
+}
+
+/* CloverChunk::ppcg_init, tea_leaf_kernel_ocl.cpp:327-344 */
+void oracle_ppcg_init(const double* alphas, const double* betas, double theta,
+                      int n) {
+  store_coefs(alphas, betas, n);
+  C.theta_ppcg = theta;
+}
+
+/* tea_leaf_ppcg_solve_init_sd, tea_leaf_ppcg_cl.cl:4-60 (z is not written) */
+void oracle_ppcg_init_sd(void) {
+  const int H = C.H;
+  const double theta = C.theta_ppcg;
+  double* zl = C.ztmp;
+  if (C.prec == ORC_PREC_JAC_BLOCK) block_solve(C.r, zl);
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      if (C.prec == ORC_PREC_JAC_BLOCK)
+        C.sd[c] = zl[c] / theta;
+      else if (C.prec == ORC_PREC_JAC_DIAG)
+        C.sd[c] = C.r[c] * C.Mi[c] / theta;
+      else
+        C.sd[c] = C.r[c] / theta;
+    }
+}
+
+/* One inner step on a single chunk: CloverChunk::tea_leaf_ppcg_inner_kernel
+ * (tea_leaf_kernel_ocl.cpp:352-411) with every neighbour an external face,
+ * i.e. both kernels over the interior: ppcg_solve_update_r then
+ * ppcg_solve_calc_sd with coefficient index step-1
+ * (tea_leaf_ppcg_cl.cl:62-155). */
+void oracle_ppcg_inner(int step) {
+  const int H = C.H;
+  const int s = step - 1;
+  const double a = C.ch_alphas[s], b = C.ch_betas[s];
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      C.u[c] = C.u[c] + C.sd[c];
+    }
+  /* r -= A sd reads sd only, so a second sweep is equivalent */
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      const double result = smvp_at(C.sd, c);
+      C.r[c] = C.r[c] - result;
+    }
+  double* zl = C.ztmp;
+  if (C.prec == ORC_PREC_JAC_BLOCK) block_solve(C.r, zl);
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      if (C.prec == ORC_PREC_JAC_BLOCK)
+        C.sd[c] = a * C.sd[c] + b * zl[c];
+      else if (C.prec == ORC_PREC_JAC_DIAG)
+        C.sd[c] = a * C.sd[c] + b * C.r[c] * C.Mi[c];
+      else
+        C.sd[c] = a * C.sd[c] + b * C.r[c];
+    }
+}
+
+/* CloverChunk::tea_leaf_jacobi_solve_kernel (tea_leaf_kernel_ocl.cpp:222-229):
+ * jacobi_copy_u into Mi (the reference reuses vector_Mi as un,
+ * ocl_kernels.cpp:576-585), then jacobi_solve (tea_leaf_jacobi_cl.cl:15-42). */
+void oracle_jacobi_solve(double* error) {
+  const int H = C.H;
+  double* un = C.Mi;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) un[IDX(col, row)] = C.u[IDX(col, row)];
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      const long xs = C.xs;
+      C.u[c] = (C.u0[c] + C.Kx[c + 1] * un[c + 1] + C.Kx[c] * un[c - 1] +
+                C.Ky[c + xs] * un[c + xs] + C.Ky[c] * un[c - xs]) /
+               (1.0 + (C.Kx[c] + C.Kx[c + 1]) + (C.Ky[c] + C.Ky[c + xs]));
+      SCR(0, col, row) = fabs(C.u[c] - un[c]);
+    }
+  *error = reduce_scratch(0);
+}
+
+/* tea_leaf_finalise, tea_leaf_common_cl.cl:4-15 */
+void oracle_finalise_kernel(void) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      C.energy1[c] = C.u[c] / C.density[c];
+    }
+}
+
+/* field_summary, field_summary_cl.cl:3-43, bound to volume, density,
+ * energy1, u (ocl_kernels.cpp:466-469) */
+void oracle_field_summary(double* vol, double* mass, double* ie, double* temp) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      const double cell_vol = C.volume[c];
+      const double cell_mass = cell_vol * C.density[c];
+      SCR(0, col, row) = cell_vol;
+      SCR(1, col, row) = cell_mass;
+      SCR(2, col, row) = cell_mass * C.energy1[c];
+      SCR(3, col, row) = cell_mass * C.u[c];
+    }
+  *vol = reduce_scratch(0);
+  *mass = reduce_scratch(1);
+  *ie = reduce_scratch(2);
+  *temp = reduce_scratch(3);
+}
+
+/* update_halo_{bottom,top,left,right} (update_halo_cl.cl:3-69) in the order
+ * of CloverChunk::update_array (update_halo_kernel_ocl.cpp:14-46), for
+ * density, energy0, energy1 (update_halo_kernel_ocl.cpp:48-62); every face is
+ * external on a single chunk. */
+static void reflect(double* a, int depth) {
+  const int H = C.H;
+  for (int row = H - depth; row < H; row++)
+    for (int col = H - depth; col <= C.x_max + H - 1 + depth; col++) {
+      const int src = 1 + (H - row - 1) * 2;
+      a[IDX(col, row)] = 1 * a[IDX(col, row + src)];
+    }
+  for (int row = H - depth; row < H; row++)
+    for (int col = H - depth; col <= C.x_max + H - 1 + depth; col++) {
+      const int src = C.y_max;
+      const int dst = C.y_max + (H - row - 1) * 2 + 1;
+      a[IDX(col, row + dst)] = a[IDX(col, row + src)];
+    }
+  for (int row = H - depth; row <= C.y_max + H - 1 + depth; row++)
+    for (int col = H - depth; col < H; col++) {
+      const int src = 1 + (H - col - 1) * 2;
+      a[IDX(col, row)] = 1 * a[IDX(col + src, row)];
+    }
+  for (int row = H - depth; row <= C.y_max + H - 1 + depth; row++)
+    for (int col = H - depth; col < H; col++) {
+      const int src = C.x_max;
+      const int dst = C.x_max + (H - col - 1) * 2 + 1;
+      a[IDX(col + dst, row)] = a[IDX(col + src, row)];
+    }
+}
+
+void oracle_update_halo(const int* fields, int depth) {
+  if (depth < 1 || depth > C.H) return;
+  if (fields[ORC_FIELD_DENSITY - 1] == 1) reflect(C.density, depth);
+  if (fields[ORC_FIELD_ENERGY0 - 1] == 1) reflect(C.energy0, depth);
+  if (fields[ORC_FIELD_ENERGY1 - 1] == 1) reflect(C.energy1, depth);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Field access                                                             */
+/* ------------------------------------------------------------------------ */
+
+static double* field_ptr(int f) {
+  switch (f) {
+    case ORC_FIELD_DENSITY: return C.density;
+    case ORC_FIELD_ENERGY0: return C.energy0;
+    case ORC_FIELD_ENERGY1: return C.energy1;
+    case ORC_FIELD_U: return C.u;
+    case ORC_FIELD_P: return C.p;
+    case ORC_FIELD_SD: return C.sd;
+    case ORC_FIELD_R: return C.r;
+    case ORC_FIELD_U0: return C.u0;
+    case ORC_FIELD_W: return C.w;
+    case ORC_FIELD_Z: return C.z;
+    case ORC_FIELD_MI: return C.Mi;
+    case ORC_FIELD_KX: return C.Kx;
+    case ORC_FIELD_KY: return C.Ky;
+    case ORC_FIELD_CP: return C.cp;
+    case ORC_FIELD_BFP: return C.bfp;
+    case ORC_FIELD_VOLUME: return C.volume;
+    default: return NULL;
+  }
+}
+
+int oracle_read_field(int f, double* out) {
+  double* a = field_ptr(f);
+  if (!a || !C_ready) return -1;
+  for (int y = 0; y < C.y_max; y++)
+    for (int x = 0; x < C.x_max; x++)
+      out[(long)y * C.x_max + x] = a[IDX(x + C.H, y + C.H)];
+  return 0;
+}
+
+int oracle_write_field(int f, const double* in) {
+  double* a = field_ptr(f);
+  if (!a || !C_ready) return -1;
+  for (int y = 0; y < C.y_max; y++)
+    for (int x = 0; x < C.x_max; x++)
+      a[IDX(x + C.H, y + C.H)] = in[(long)y * C.x_max + x];
+  return 0;
+}
+
+int oracle_read_field_padded(int f, double* out, long n) {
+  double* a = field_ptr(f);
+  const long need = (long)C.xs * C.ys;
+  if (!a || !C_ready || n < need) return -1;
+  memcpy(out, a, sizeof(double) * (size_t)need);
+  return 0;
+}
+
+int oracle_write_field_padded(int f, const double* in, long n) {
+  double* a = field_ptr(f);
+  const long need = (long)C.xs * C.ys;
+  if (!a || !C_ready || n < need) return -1;
+  memcpy(a, in, sizeof(double) * (size_t)need);
+  return 0;
+}
+
+int oracle_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}

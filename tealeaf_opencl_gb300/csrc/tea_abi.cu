@@ -1,0 +1,835 @@
+// The C ABI of libtealeaf_gb300.so: the reference's extern "C" entry points
+// (tea_leaf_kernel_ocl.cpp, field_summary_kernel_ocl.cpp,
+// update_halo_kernel_ocl.cpp, ocl_init.cpp, initialise_chunk_kernel_ocl.cpp,
+// generate_chunk_kernel_ocl.cpp, set_field_kernel_ocl.cpp, ocl_errors.cpp,
+// ocl_pack.cpp) on top of the CUDA kernels, plus the chunk's lifecycle.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/tealeaf_gb300.h"
+#include "tea_internal.h"
+
+namespace tea {
+
+static Chunk g_chunk;
+Chunk& chunk() { return g_chunk; }
+
+// ---------------------------------------------------------------------------
+// errors, launch accounting, profiling
+// ---------------------------------------------------------------------------
+
+static int g_abort_on_error = 1;
+static int g_err_code = 0;
+static std::string g_err_msg;
+static long long g_launches = 0;
+
+void fail(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (g_err_code == 0) {
+    g_err_code = code;
+    g_err_msg = buf;
+  }
+  fprintf(stderr, "@@@@@\nFatal error in libtealeaf_gb300: %s\n", buf);
+  if (g_abort_on_error) {
+    fprintf(stderr, "Exiting\n");
+    abort();
+  }
+}
+
+int error_code() { return g_err_code; }
+
+bool check_cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  fail(2, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+  return false;
+}
+
+void count_launch(const char*) { g_launches++; }
+
+struct ProfEntry {
+  long long calls = 0;
+  double ms = 0.0;
+};
+static std::map<std::string, ProfEntry> g_prof;
+static cudaEvent_t g_prof_ev[2] = {nullptr, nullptr};
+
+// Optional timing of one named kernel inside a running workload: event
+// pairs recorded around each of its launches on the library's stream, read
+// back in batches without serialising the other work.
+static std::string g_timed_name;
+static std::vector<cudaEvent_t> g_timed_ev;
+static size_t g_timed_used = 0;
+static double g_timed_ms = 0.0;
+static long long g_timed_n = 0;
+
+static void timed_drain() {
+  if (g_timed_used == 0) return;
+  cudaEventSynchronize(g_timed_ev[2 * g_timed_used - 1]);
+  for (size_t i = 0; i < g_timed_used; i++) {
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, g_timed_ev[2 * i], g_timed_ev[2 * i + 1]);
+    g_timed_ms += ms;
+    g_timed_n++;
+  }
+  g_timed_used = 0;
+}
+
+void profile_begin(const char* name) {
+  Chunk& c = chunk();
+  if (!g_timed_name.empty() && g_timed_name == name) {
+    if (g_timed_ev.empty()) {
+      g_timed_ev.resize(2 * 1024);
+      for (auto& e : g_timed_ev) cudaEventCreate(&e);
+    }
+    if (2 * (g_timed_used + 1) > g_timed_ev.size()) timed_drain();
+    cudaEventRecord(g_timed_ev[2 * g_timed_used], c.stream);
+  }
+  if (!c.profiler_on) return;
+  if (!g_prof_ev[0]) {
+    cudaEventCreate(&g_prof_ev[0]);
+    cudaEventCreate(&g_prof_ev[1]);
+  }
+  cudaEventRecord(g_prof_ev[0], c.stream);
+}
+
+// Waits for the kernel, as the reference's profiled enqueueKernel does
+// (ocl_errors.cpp:75-122).
+void profile_end(const char* name) {
+  Chunk& c = chunk();
+  if (!g_timed_name.empty() && g_timed_name == name) {
+    cudaEventRecord(g_timed_ev[2 * g_timed_used + 1], c.stream);
+    g_timed_used++;
+  }
+  if (!c.profiler_on) return;
+  cudaEventRecord(g_prof_ev[1], c.stream);
+  cudaEventSynchronize(g_prof_ev[1]);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, g_prof_ev[0], g_prof_ev[1]);
+  ProfEntry& e = g_prof[name];
+  e.calls++;
+  e.ms += ms;
+}
+
+// ---------------------------------------------------------------------------
+// chunk
+// ---------------------------------------------------------------------------
+
+int reduction_rows(int x_max, int y_max) {
+  const long long nsx = (x_max + 255) / 256;
+  const long long nsy16 = (y_max + 15) / 16;
+  return (nsx * nsy16 >= 1216) ? 16 : 4;
+}
+
+Dev Chunk::dev() const {
+  Dev d;
+  memset(&d, 0, sizeof(d));
+  d.x_max = x_max;
+  d.y_max = y_max;
+  d.H = H;
+  d.S = S;
+  d.xs = x_max + 2 * H;
+  d.ys = y_max + 2 * H;
+  d.prec = prec;
+  d.block_top_check = (y_max % 4) != 0;
+  d.ntx = (x_max + kTileW - 1) / kTileW;
+  d.nsx = (d.ntx + kTilesPerSuper - 1) / kTilesPerSuper;
+  d.nty = (y_max + TH - 1) / TH;
+  d.ns = d.nsx * d.nty;
+  d.density = density.f;
+  d.energy0 = energy0.f;
+  d.energy1 = energy1.f;
+  d.volume = volume.f;
+  d.u = u.f;
+  d.u0 = u0.f;
+  d.p = p.f;
+  d.r = r.f;
+  d.w = w.f;
+  d.Mi = Mi.f;
+  d.Kx = Kx.f;
+  d.Ky = Ky.f;
+  d.sd = sd.f;
+  d.z = z.f;
+  d.cp = cp.f;
+  d.bfp = bfp.f;
+  d.un = Mi.f;  // the reference reuses vector_Mi as Jacobi's un
+  d.cellx = cellx;
+  d.celly = celly;
+  d.celldx = celldx;
+  d.celldy = celldy;
+  d.vertexx = vertexx;
+  d.vertexy = vertexy;
+  d.vertexdx = vertexdx;
+  d.vertexdy = vertexdy;
+  return d;
+}
+
+Red Chunk::red() const {
+  Red rr;
+  rr.partials = red_partials;
+  rr.stride = red_stride;
+  rr.counter = red_counter;
+  rr.result = red_result;
+  return rr;
+}
+
+static void free_chunk(Chunk& c) {
+  if (!c.ready) return;
+  resident_release();
+  Field* l[] = {&c.density, &c.energy0, &c.energy1, &c.volume, &c.u, &c.u0,
+                &c.p,       &c.r,       &c.w,       &c.Mi,     &c.Kx, &c.Ky,
+                &c.sd,      &c.z,       &c.cp,      &c.bfp};
+  for (Field* f : l) {
+    cudaFree(f->base);
+    f->base = f->f = nullptr;
+  }
+  double** one[] = {&c.cellx,   &c.celly,   &c.celldx,   &c.celldy,
+                    &c.vertexx, &c.vertexy, &c.vertexdx, &c.vertexdy,
+                    &c.red_partials, &c.red_result};
+  for (double** p : one) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  cudaFree(c.red_counter);
+  c.red_counter = nullptr;
+  cudaFreeHost(c.host_result);
+  c.host_result = nullptr;
+  free(c.cheby_alpha_h);
+  free(c.cheby_beta_h);
+  free(c.ppcg_alpha_h);
+  free(c.ppcg_beta_h);
+  c.cheby_alpha_h = c.cheby_beta_h = c.ppcg_alpha_h = c.ppcg_beta_h = nullptr;
+  if (c.stream) cudaStreamDestroy(c.stream);
+  c.stream = nullptr;
+  c.ready = false;
+}
+
+static bool alloc_field(Chunk& c, Field& f) {
+  // the offset makes padded column H of every row 256-byte aligned
+  const long long off = (32 - (c.H % 32)) % 32;
+  const size_t n = (size_t)(off + c.rows * c.S + 32);
+  if (!check_cuda(cudaMalloc(&f.base, n * sizeof(double)), "cudaMalloc field"))
+    return false;
+  if (!check_cuda(cudaMemsetAsync(f.base, 0, n * sizeof(double), c.stream),
+                  "cudaMemset field"))
+    return false;
+  f.f = f.base + off;
+  return true;
+}
+
+struct Config {
+  bool set = false;
+  int halo = 1, solver = SOLVER_JACOBI, prec = PREC_NONE, profiler = 0;
+};
+static Config g_config;
+
+// matchParam / readInt / paramEnabled (ocl_strings.cpp:7-37, :53-75,
+// :127-132): first line without '!' that contains the name; its value is
+// the text after the first '='.
+static std::string match_param(const std::string& text, const char* name) {
+  std::istringstream in(text);
+  std::string line;
+  while (std::getline(in, line)) {
+    if (line.find('!') != std::string::npos) continue;
+    if (line.find(name) != std::string::npos) {
+      const size_t eq = line.find('=');
+      if (eq != std::string::npos) return line.substr(eq + 1);
+      return std::string(name);
+    }
+  }
+  return std::string();
+}
+
+static bool config_from_tea_in(Config* cfg) {
+  std::ifstream f("tea.in");
+  if (!f.is_open()) {
+    fail(3, "Input file not found");
+    return false;
+  }
+  std::stringstream ss;
+  ss << f.rdbuf();
+  const std::string text = ss.str();
+  cfg->profiler = !match_param(text, "profiler_on").empty();
+  {
+    std::stringstream conv(match_param(text, "halo_depth"));
+    int h = -1;
+    if (!(conv >> h)) h = -1;
+    cfg->halo = h;
+    if (h < 1) {
+      fail(3, "Halo exchange depth unspecified or was too small");
+      return false;
+    }
+  }
+  if (!match_param(text, "tl_use_ppcg").empty())
+    cfg->solver = SOLVER_PPCG;
+  else if (!match_param(text, "tl_use_chebyshev").empty())
+    cfg->solver = SOLVER_CHEBY;
+  else if (!match_param(text, "tl_use_cg").empty())
+    cfg->solver = SOLVER_CG;
+  else
+    cfg->solver = SOLVER_JACOBI;
+  std::string prec = match_param(text, "tl_preconditioner_type");
+  std::transform(prec.begin(), prec.end(), prec.begin(), ::tolower);
+  if (prec.find("jac_diag") != std::string::npos)
+    cfg->prec = PREC_JAC_DIAG;
+  else if (prec.find("jac_block") != std::string::npos)
+    cfg->prec = PREC_JAC_BLOCK;
+  else
+    cfg->prec = PREC_NONE;
+  return true;
+}
+
+static bool init_chunk(int x_max, int y_max, const Config& cfg) {
+  Chunk& c = chunk();
+  free_chunk(c);
+  c = Chunk();
+  if (x_max < 1 || y_max < 1) {
+    fail(4, "invalid chunk size %d x %d", x_max, y_max);
+    return false;
+  }
+  c.x_max = x_max;
+  c.y_max = y_max;
+  c.H = cfg.halo;
+  c.solver = cfg.solver;
+  c.prec = cfg.prec;
+  c.profiler_on = cfg.profiler != 0;
+  c.TH = reduction_rows(x_max, y_max);
+  c.S = ((long long)(x_max + 2 * c.H + 1 + 31) / 32) * 32;
+  c.rows = y_max + 2 * c.H + 1;
+  if (!check_cuda(cudaGetDevice(&c.device), "cudaGetDevice")) return false;
+  cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, c.device);
+  if (!check_cuda(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking),
+                  "cudaStreamCreate"))
+    return false;
+  c.ready = true;  // so that free_chunk releases partial allocations
+  Field* l[] = {&c.density, &c.energy0, &c.energy1, &c.volume, &c.u, &c.u0,
+                &c.p,       &c.r,       &c.w,       &c.Mi,     &c.Kx, &c.Ky,
+                &c.sd,      &c.z,       &c.cp,      &c.bfp};
+  for (Field* f : l)
+    if (!alloc_field(c, *f)) return false;
+  const int n1 = std::max(x_max, y_max) + 2 * c.H + 2;
+  double** one[] = {&c.cellx,   &c.celly,   &c.celldx,   &c.celldy,
+                    &c.vertexx, &c.vertexy, &c.vertexdx, &c.vertexdy};
+  for (double** p : one) {
+    if (!check_cuda(cudaMalloc(p, n1 * sizeof(double)), "cudaMalloc 1d"))
+      return false;
+    cudaMemsetAsync(*p, 0, n1 * sizeof(double), c.stream);
+  }
+  // supertile count is largest for the smallest tile height
+  const long long ntx = (x_max + kTileW - 1) / kTileW;
+  const long long nsx = (ntx + kTilesPerSuper - 1) / kTilesPerSuper;
+  c.red_stride = nsx * ((y_max + 3) / 4) + 1;
+  if (!check_cuda(cudaMalloc(&c.red_partials, 8 * c.red_stride * sizeof(double)),
+                  "cudaMalloc partials") ||
+      !check_cuda(cudaMalloc(&c.red_result, 8 * sizeof(double)),
+                  "cudaMalloc result") ||
+      !check_cuda(cudaMalloc(&c.red_counter, 8 * sizeof(unsigned int)),
+                  "cudaMalloc counter") ||
+      !check_cuda(cudaMallocHost(&c.host_result, 8 * sizeof(double)),
+                  "cudaMallocHost"))
+    return false;
+  cudaMemsetAsync(c.red_counter, 0, 8 * sizeof(unsigned int), c.stream);
+  cudaMemsetAsync(c.red_result, 0, 8 * sizeof(double), c.stream);
+  return check_cuda(cudaStreamSynchronize(c.stream), "chunk allocation");
+}
+
+static bool need_chunk(const char* who) {
+  if (!chunk().ready) {
+    fail(5, "%s called before initialise_ocl_", who);
+    return false;
+  }
+  return true;
+}
+
+// Copies the reduced values back: every scalar-returning call is
+// synchronous, like reduceValue (ocl_reduction.hpp:6-35).
+static bool fetch(int nv, double* out) {
+  Chunk& c = chunk();
+  if (!check_cuda(cudaMemcpyAsync(c.host_result, c.red_result,
+                                  nv * sizeof(double), cudaMemcpyDeviceToHost,
+                                  c.stream),
+                  "reduction read-back") ||
+      !check_cuda(cudaStreamSynchronize(c.stream), "reduction sync")) {
+    for (int i = 0; i < nv; i++) out[i] = NAN;
+    return false;
+  }
+  for (int i = 0; i < nv; i++) out[i] = c.host_result[i];
+  return true;
+}
+
+static Field* field_by_id(Chunk& c, int id) {
+  switch (id) {
+    case 1: return &c.density;
+    case 2: return &c.energy0;
+    case 3: return &c.energy1;
+    case 4: return &c.u;
+    case 5: return &c.p;
+    case 6: return &c.sd;
+    case 7: return &c.r;
+    case 8: return &c.u0;
+    case 9: return &c.w;
+    case 10: return &c.z;
+    case 11: return &c.Mi;
+    case 12: return &c.Kx;
+    case 13: return &c.Ky;
+    case 14: return &c.cp;
+    case 15: return &c.bfp;
+    case 16: return &c.volume;
+    default: return nullptr;
+  }
+}
+
+static bool store_coefs(const double* a, const double* b, int n, double** ah,
+                        double** bh) {
+  free(*ah);
+  free(*bh);
+  *ah = (double*)malloc(sizeof(double) * (size_t)std::max(n, 1));
+  *bh = (double*)malloc(sizeof(double) * (size_t)std::max(n, 1));
+  if (!*ah || !*bh) {
+    fail(6, "out of host memory for %d coefficients", n);
+    return false;
+  }
+  if (n > 0) {
+    memcpy(*ah, a, sizeof(double) * (size_t)n);
+    memcpy(*bh, b, sizeof(double) * (size_t)n);
+  }
+  return true;
+}
+
+}  // namespace tea
+
+using namespace tea;
+
+// ===========================================================================
+// Part 1: reference entry points
+// ===========================================================================
+
+extern "C" void initialise_ocl_(int* x_min, int* x_max, int* y_min, int* y_max) {
+  Config cfg = g_config;
+  if (!cfg.set && !config_from_tea_in(&cfg)) return;
+  init_chunk(*x_max - *x_min + 1, *y_max - *y_min + 1, cfg);
+}
+
+extern "C" void initialise_chunk_kernel_ocl_(double* d_xmin, double* d_ymin,
+                                             double* d_dx, double* d_dy) {
+  if (!need_chunk("initialise_chunk_kernel_ocl_")) return;
+  Chunk& c = chunk();
+  c.celldx_h = *d_dx;
+  c.celldy_h = *d_dy;
+  launch_initialise_chunk(c, *d_xmin, *d_ymin, *d_dx, *d_dy);
+  check_cuda(cudaStreamSynchronize(c.stream), "initialise_chunk");
+}
+
+extern "C" void generate_chunk_kernel_ocl_(
+    const int* number_of_states, const double* state_density,
+    const double* state_energy, const double* state_xmin,
+    const double* state_xmax, const double* state_ymin,
+    const double* state_ymax, const double* state_radius,
+    const int* state_geometry, const int* g_rect, const int* g_circ,
+    const int* g_point) {
+  if (!need_chunk("generate_chunk_kernel_ocl_")) return;
+  Chunk& c = chunk();
+  launch_generate_init(c, state_density[0], state_energy[0]);
+  for (int s = 1; s < *number_of_states; s++)
+    launch_generate_state(c, state_density[s], state_energy[s], state_xmin[s],
+                          state_xmax[s], state_ymin[s], state_ymax[s],
+                          state_radius[s], state_geometry[s], *g_rect, *g_circ,
+                          *g_point);
+  launch_init_u(c, c.energy0.f);
+}
+
+extern "C" void set_field_kernel_ocl_(void) {
+  if (!need_chunk("set_field_kernel_ocl_")) return;
+  launch_set_field(chunk());
+}
+
+extern "C" void field_summary_kernel_ocl_(double* vol, double* mass, double* ie,
+                                          double* temp) {
+  double out[4] = {NAN, NAN, NAN, NAN};
+  if (need_chunk("field_summary_kernel_ocl_")) {
+    launch_field_summary(chunk());
+    fetch(4, out);
+  }
+  *vol = out[0];
+  *mass = out[1];
+  *ie = out[2];
+  *temp = out[3];
+}
+
+extern "C" void update_halo_kernel_ocl_(const int* chunk_neighbours,
+                                        const int* fields, const int* depth) {
+  if (!need_chunk("update_halo_kernel_ocl_")) return;
+  Chunk& c = chunk();
+  for (int f = 0; f < 4; f++) {
+    if (chunk_neighbours[f] != TEA_EXTERNAL_FACE) {
+      fail(7, "update_halo_kernel_ocl_: only a single chunk (all faces "
+              "external) is supported");
+      return;
+    }
+  }
+  if (*depth < 1 || *depth > c.H) {
+    fail(7, "update_halo_kernel_ocl_: depth %d outside 1..%d", *depth, c.H);
+    return;
+  }
+  const int mask = (fields[TEA_FIELD_DENSITY - 1] == 1 ? 1 : 0) |
+                   (fields[TEA_FIELD_ENERGY0 - 1] == 1 ? 2 : 0) |
+                   (fields[TEA_FIELD_ENERGY1 - 1] == 1 ? 4 : 0);
+  launch_update_halo(c, mask, *depth);
+}
+
+extern "C" void tea_leaf_common_init_kernel_ocl_(const int* coefficient,
+                                                 double* dt, double* rx,
+                                                 double* ry, int* zero_boundary,
+                                                 int* reflective_boundary) {
+  if (!need_chunk("tea_leaf_common_init_kernel_ocl_")) return;
+  Chunk& c = chunk();
+  if (*coefficient != TEA_COEF_CONDUCTIVITY &&
+      *coefficient != TEA_COEF_RECIP_CONDUCTIVITY) {
+    fail(8, "Unknown coefficient %d passed to tea leaf", *coefficient);
+    return;
+  }
+  // calcrxry (tea_leaf_kernel_ocl.cpp:8-32): celldx/celldy never change, so
+  // the host copies kept at initialise_chunk time are used.
+  const double dx = c.celldx_h, dy = c.celldy_h;
+  *rx = *dt / (dx * dx);
+  *ry = *dt / (dy * dy);
+  launch_init_common(c, *coefficient, *rx, *ry);
+  if (!*reflective_boundary) launch_zero_boundary(c, zero_boundary);
+  launch_init_u(c, c.energy1.f);
+}
+
+extern "C" void tea_leaf_calc_residual_ocl_(void) {
+  if (!need_chunk("tea_leaf_calc_residual_ocl_")) return;
+  launch_calc_residual(chunk());
+}
+
+extern "C" void tea_leaf_calc_2norm_kernel_ocl_(int* norm_array, double* norm) {
+  *norm = NAN;
+  if (!need_chunk("tea_leaf_calc_2norm_kernel_ocl_")) return;
+  Chunk& c = chunk();
+  const double *a, *b;
+  if (*norm_array == 0) {
+    a = b = c.u0.f;
+  } else if (*norm_array == 1) {
+    a = b = c.r.f;
+  } else if (*norm_array == 2) {
+    a = c.r.f;
+    b = (c.prec == PREC_NONE) ? c.r.f : c.z.f;
+  } else {
+    fail(9, "Invalid value '%d' for norm_array passed, should be 0 for u0, 1 "
+            "for r, 2 for r*z",
+         *norm_array);
+    return;
+  }
+  launch_dot(c, a, b);
+  fetch(1, norm);
+}
+
+extern "C" void tea_leaf_cg_init_kernel_ocl_(double* rro) {
+  *rro = NAN;
+  if (!need_chunk("tea_leaf_cg_init_kernel_ocl_")) return;
+  Chunk& c = chunk();
+  if (c.solver == SOLVER_JACOBI) {
+    fail(10, "tea_leaf_cg_init_kernel_ocl_ called with the Jacobi solver");
+    return;
+  }
+  if (c.prec == PREC_JAC_BLOCK)
+    launch_block_init(c);
+  else if (c.prec == PREC_JAC_DIAG)
+    launch_init_jac_diag(c);
+  launch_cg_init_p(c);
+  fetch(1, rro);
+}
+
+extern "C" void tea_leaf_cg_calc_w_kernel_ocl_(double* pw) {
+  *pw = NAN;
+  if (!need_chunk("tea_leaf_cg_calc_w_kernel_ocl_")) return;
+  launch_cg_calc_w(chunk());
+  fetch(1, pw);
+}
+
+extern "C" void tea_leaf_cg_calc_ur_kernel_ocl_(double* alpha, double* rrn) {
+  const double a = *alpha;
+  *rrn = NAN;
+  if (!need_chunk("tea_leaf_cg_calc_ur_kernel_ocl_")) return;
+  launch_cg_calc_ur(chunk(), a);
+  fetch(1, rrn);
+}
+
+extern "C" void tea_leaf_cg_calc_p_kernel_ocl_(double* beta) {
+  if (!need_chunk("tea_leaf_cg_calc_p_kernel_ocl_")) return;
+  launch_cg_calc_p(chunk(), *beta);
+}
+
+extern "C" void tea_leaf_cheby_init_kernel_ocl_(const double* ch_alphas,
+                                                const double* ch_betas,
+                                                int* n_coefs, const double* rx,
+                                                const double* ry,
+                                                const double* theta) {
+  (void)rx;
+  (void)ry;
+  if (!need_chunk("tea_leaf_cheby_init_kernel_ocl_")) return;
+  Chunk& c = chunk();
+  if (!store_coefs(ch_alphas, ch_betas, *n_coefs, &c.cheby_alpha_h,
+                   &c.cheby_beta_h))
+    return;
+  c.n_cheby = *n_coefs;
+  c.cheby_theta = *theta;
+  launch_cheby_init_p(c, *theta);
+  launch_cheby_calc_u(c);
+}
+
+extern "C" void tea_leaf_cheby_iterate_kernel_ocl_(const int* cheby_calc_step) {
+  if (!need_chunk("tea_leaf_cheby_iterate_kernel_ocl_")) return;
+  Chunk& c = chunk();
+  const int s = *cheby_calc_step - 1;
+  if (s < 0 || s >= c.n_cheby) {
+    fail(11, "Chebyshev step %d outside the %d stored coefficients",
+         *cheby_calc_step, c.n_cheby);
+    return;
+  }
+  launch_cheby_calc_p(c, c.cheby_alpha_h[s], c.cheby_beta_h[s]);
+  launch_cheby_calc_u(c);
+}
+
+extern "C" void tea_leaf_ppcg_init_ocl_(const double* ch_alphas,
+                                        const double* ch_betas, double* theta,
+                                        int* n_inner_steps) {
+  if (!need_chunk("tea_leaf_ppcg_init_ocl_")) return;
+  Chunk& c = chunk();
+  if (!store_coefs(ch_alphas, ch_betas, *n_inner_steps, &c.ppcg_alpha_h,
+                   &c.ppcg_beta_h))
+    return;
+  c.n_ppcg = *n_inner_steps;
+  c.ppcg_theta = *theta;
+}
+
+extern "C" void tea_leaf_ppcg_init_sd_kernel_ocl_(void) {
+  if (!need_chunk("tea_leaf_ppcg_init_sd_kernel_ocl_")) return;
+  Chunk& c = chunk();
+  launch_ppcg_init_sd(c, c.ppcg_theta);
+}
+
+extern "C" void tea_leaf_ppcg_inner_kernel_ocl_(int* inner_step,
+                                                int* bounds_extra,
+                                                const int* chunk_neighbours) {
+  (void)bounds_extra;
+  if (!need_chunk("tea_leaf_ppcg_inner_kernel_ocl_")) return;
+  Chunk& c = chunk();
+  for (int f = 0; f < 4; f++) {
+    if (chunk_neighbours[f] != TEA_EXTERNAL_FACE) {
+      fail(7, "tea_leaf_ppcg_inner_kernel_ocl_: only a single chunk (all "
+              "faces external) is supported");
+      return;
+    }
+  }
+  const int s = *inner_step - 1;
+  if (s < 0 || s >= c.n_ppcg) {
+    fail(11, "PPCG inner step %d outside the %d stored coefficients",
+         *inner_step, c.n_ppcg);
+    return;
+  }
+  launch_ppcg_update_r(c);
+  launch_ppcg_calc_sd(c, c.ppcg_alpha_h[s], c.ppcg_beta_h[s]);
+}
+
+extern "C" void tea_leaf_jacobi_solve_kernel_ocl_(double* error) {
+  *error = NAN;
+  if (!need_chunk("tea_leaf_jacobi_solve_kernel_ocl_")) return;
+  Chunk& c = chunk();
+  launch_jacobi_copy_u(c);
+  launch_jacobi_solve(c);
+  fetch(1, error);
+}
+
+extern "C" void tea_leaf_common_finalise_kernel_ocl_(void) {
+  if (!need_chunk("tea_leaf_common_finalise_kernel_ocl_")) return;
+  launch_finalise(chunk());
+}
+
+extern "C" void print_opencl_profiling_info_(void) {
+  Chunk& c = chunk();
+  if (!c.profiler_on) return;
+  fprintf(stdout, "@@@@@ CUDA Profiling information @@@@@\n");
+  for (auto& kv : g_prof) {
+    if (kv.second.calls)
+      fprintf(stdout, "%30s : %10.3f ms (%.2f us avg. over %lld calls)\n",
+              kv.first.c_str(), kv.second.ms,
+              1e3 * kv.second.ms / (double)kv.second.calls, kv.second.calls);
+  }
+}
+
+static void pack_unpack(int* fields, const char* who) {
+  int n = 0;
+  for (int i = 0; i < 7; i++) n += fields[i];
+  if (n < 1) return;  // nothing exchanged, as ocl_pack.cpp:24-29
+  fail(12, "%s: MPI halo exchange is not supported (single chunk)", who);
+}
+
+extern "C" void ocl_pack_buffers_(int* fields, int* offsets, int* depth,
+                                  int* face, double* host_buffer) {
+  (void)offsets;
+  (void)depth;
+  (void)face;
+  (void)host_buffer;
+  pack_unpack(fields, "ocl_pack_buffers_");
+}
+
+extern "C" void ocl_unpack_buffers_(int* fields, int* offsets, int* depth,
+                                    int* face, double* host_buffer) {
+  (void)offsets;
+  (void)depth;
+  (void)face;
+  (void)host_buffer;
+  pack_unpack(fields, "ocl_unpack_buffers_");
+}
+
+// ===========================================================================
+// Part 2: additions
+// ===========================================================================
+
+extern "C" int tea_gb300_configure(int halo_depth, int solver,
+                                   int preconditioner, int profiler_on) {
+  if (halo_depth < 1 || solver < 1 || solver > 4 || preconditioner < 1 ||
+      preconditioner > 3)
+    return -1;
+  g_config.set = true;
+  g_config.halo = halo_depth;
+  g_config.solver = solver;
+  g_config.prec = preconditioner;
+  g_config.profiler = profiler_on;
+  return 0;
+}
+
+extern "C" void tea_gb300_set_abort_on_error(int a) { g_abort_on_error = a; }
+
+extern "C" int tea_gb300_last_error(char* msg, int len) {
+  const int code = g_err_code;
+  if (msg && len > 0) {
+    strncpy(msg, g_err_msg.c_str(), (size_t)len - 1);
+    msg[len - 1] = 0;
+  }
+  g_err_code = 0;
+  g_err_msg.clear();
+  return code;
+}
+
+extern "C" void tea_gb300_finalise(void) { free_chunk(chunk()); }
+
+static int copy_field(int id, double* host, const double* in, bool padded) {
+  if (!need_chunk("field access")) return -1;
+  Chunk& c = chunk();
+  Field* f = field_by_id(c, id);
+  if (!f) {
+    fail(13, "unknown field %d", id);
+    return -1;
+  }
+  const int off = padded ? 0 : c.H;
+  const int w = padded ? c.x_max + 2 * c.H : c.x_max;
+  const int h = padded ? c.y_max + 2 * c.H : c.y_max;
+  double* dev = f->f + (long long)off * c.S + off;
+  cudaError_t e;
+  if (in)
+    e = cudaMemcpy2DAsync(dev, c.S * sizeof(double), in, w * sizeof(double),
+                          w * sizeof(double), h, cudaMemcpyHostToDevice,
+                          c.stream);
+  else
+    e = cudaMemcpy2DAsync(host, w * sizeof(double), dev, c.S * sizeof(double),
+                          w * sizeof(double), h, cudaMemcpyDeviceToHost,
+                          c.stream);
+  if (!check_cuda(e, "field copy")) return -1;
+  return check_cuda(cudaStreamSynchronize(c.stream), "field copy sync") ? 0 : -1;
+}
+
+extern "C" int tea_gb300_read_field(int field, double* out) {
+  return copy_field(field, out, nullptr, false);
+}
+extern "C" int tea_gb300_write_field(int field, const double* in) {
+  return copy_field(field, nullptr, in, false);
+}
+extern "C" int tea_gb300_read_field_padded(int field, double* out) {
+  return copy_field(field, out, nullptr, true);
+}
+extern "C" int tea_gb300_write_field_padded(int field, const double* in) {
+  return copy_field(field, nullptr, in, true);
+}
+
+extern "C" int tea_gb300_reduction_rows(int x_max, int y_max) {
+  return reduction_rows(x_max, y_max);
+}
+
+extern "C" long long tea_gb300_kernel_launches(void) { return g_launches; }
+
+extern "C" void* tea_gb300_stream(void) { return (void*)chunk().stream; }
+
+extern "C" int tea_gb300_chunk_info(int* x_max, int* y_max, int* halo,
+                                    int* stride) {
+  Chunk& c = chunk();
+  if (!c.ready) return -1;
+  *x_max = c.x_max;
+  *y_max = c.y_max;
+  *halo = c.H;
+  *stride = (int)c.S;
+  return 0;
+}
+
+static cudaEvent_t g_events[16] = {nullptr};
+
+extern "C" int tea_gb300_event_record(int slot) {
+  Chunk& c = chunk();
+  if (slot < 0 || slot >= 16 || !c.ready) return -1;
+  if (!g_events[slot] && !check_cuda(cudaEventCreate(&g_events[slot]), "cudaEventCreate"))
+    return -1;
+  return check_cuda(cudaEventRecord(g_events[slot], c.stream), "cudaEventRecord") ? 0 : -1;
+}
+
+extern "C" float tea_gb300_event_elapsed_ms(int a, int b) {
+  if (a < 0 || a >= 16 || b < 0 || b >= 16 || !g_events[a] || !g_events[b]) return -1.0f;
+  if (!check_cuda(cudaEventSynchronize(g_events[b]), "cudaEventSynchronize")) return -1.0f;
+  float ms = -1.0f;
+  if (!check_cuda(cudaEventElapsedTime(&ms, g_events[a], g_events[b]), "cudaEventElapsedTime"))
+    return -1.0f;
+  return ms;
+}
+
+extern "C" int tea_gb300_synchronize(void) {
+  Chunk& c = chunk();
+  if (!c.ready) return -1;
+  return check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize") ? 0 : -1;
+}
+
+extern "C" void* tea_gb300_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (!check_cuda(cudaMallocHost(&p, bytes), "cudaMallocHost")) return nullptr;
+  return p;
+}
+
+extern "C" void tea_gb300_host_free(void* p) { cudaFreeHost(p); }
+
+extern "C" int tea_gb300_kernel_timer_select(const char* name) {
+  timed_drain();
+  g_timed_name = name ? name : "";
+  g_timed_ms = 0.0;
+  g_timed_n = 0;
+  return 0;
+}
+
+extern "C" int tea_gb300_kernel_timer_read(double* total_ms, long long* launches) {
+  timed_drain();
+  *total_ms = g_timed_ms;
+  *launches = g_timed_n;
+  return 0;
+}

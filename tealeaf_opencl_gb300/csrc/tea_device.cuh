@@ -1,0 +1,204 @@
+// Device helpers shared by the tile kernels.
+//
+// Every interior kernel walks the grid in the same tiles: a tile is 32
+// interior columns (one per lane of a warp) by TH rows; a supertile is 8
+// tiles side by side (one per warp of a 256-thread block).  Blocks take
+// supertiles s = blockIdx.x, blockIdx.x + gridDim.x, ...
+//
+// Fixed summation order of every global sum (the same order the CPU oracle
+// implements in oracle_reduce):
+//   1. a lane adds its TH rows bottom to top into an accumulator starting at
+//      +0.0; rows past the interior add +0.0, lanes past it hold +0.0;
+//   2. the 32 lane sums are combined by an xor butterfly (16,8,4,2,1): every
+//      lane ends with the tile sum;
+//   3. the 8 tile sums of a supertile (0.0 for tiles past the interior) go
+//      through the same butterfly on lanes 0..7 of warp 0, lanes 8..31
+//      holding 0.0, giving the supertile sum, stored at partials[s];
+//   4. the last block to finish adds partials[t], partials[t+256], ... on
+//      thread t from +0.0, butterflies each warp, and butterflies the 8 warp
+//      sums as in 3.
+// All arithmetic is compiled with --fmad=false, so every operation rounds
+// exactly as written.
+#pragma once
+
+#include "tea_internal.h"
+
+namespace tea {
+
+__device__ __forceinline__ long long cidx(const Dev& d, int x, int y) {
+  // interior coordinates (x,y) -> offset of padded (x+H, y+H)
+  return (long long)(y + d.H) * d.S + (x + d.H);
+}
+
+__device__ __forceinline__ double bfly(double v) {
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1)
+    v = v + __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// The 5-point operator in the association every reference kernel uses
+// (e.g. tea_leaf_cg_cl.cl:59-63).
+__device__ __forceinline__ double smvp(const Dev& d, const double* x,
+                                       long long c) {
+  const long long S = d.S;
+  const double kyn = __ldg(d.Ky + c + S), kyc = __ldg(d.Ky + c);
+  const double kxe = __ldg(d.Kx + c + 1), kxc = __ldg(d.Kx + c);
+  return (1.0 + (kyn + kyc) + (kxe + kxc)) * x[c] -
+         (kyn * x[c + S] + kyc * x[c - S]) - (kxe * x[c + 1] + kxc * x[c - 1]);
+}
+
+// COEF_B of the block-Jacobi strip (tea_block_jacobi.cl:3) at offset c.
+__device__ __forceinline__ double coef_b(const Dev& d, long long c) {
+  return (1.0 + (__ldg(d.Ky + c + d.S) + __ldg(d.Ky + c)) +
+          (__ldg(d.Kx + c + 1) + __ldg(d.Kx + c)));
+}
+
+// Rows in the strip starting at interior row y (BLOCK_TOP, macros_cl.cl:6-10;
+// the reference's formula counts one halo row when H == 1 and is exact when
+// H == 2; H >= 3 uses the exact count).
+__device__ __forceinline__ int strip_rows(const Dev& d, int y) {
+  if (!d.block_top_check) return 4;
+  const int up = d.y_max - y + (d.H == 1 ? 1 : 0);
+  return up < 4 ? up : 4;
+}
+
+// block_solve_func (tea_block_jacobi.cl:6-42) for one column of one strip:
+// z = M_block^-1 r for the strip whose first cell is at offset c0.
+__device__ __forceinline__ void strip_solve(const Dev& d, long long c0,
+                                            int upper, const double rl[4],
+                                            double zl[4]) {
+  const long long S = d.S;
+  double dp0, dp1 = 0.0, dp2 = 0.0, dp3 = 0.0;
+  dp0 = rl[0] / coef_b(d, c0);
+  if (upper > 1)
+    dp1 = (rl[1] - (-__ldg(d.Ky + c0 + S)) * dp0) * __ldg(d.bfp + c0 + S);
+  if (upper > 2)
+    dp2 = (rl[2] - (-__ldg(d.Ky + c0 + 2 * S)) * dp1) *
+          __ldg(d.bfp + c0 + 2 * S);
+  if (upper > 3)
+    dp3 = (rl[3] - (-__ldg(d.Ky + c0 + 3 * S)) * dp2) *
+          __ldg(d.bfp + c0 + 3 * S);
+  double z0, z1 = 0.0, z2 = 0.0, z3 = 0.0;
+  if (upper == 4) {
+    z3 = dp3;
+    z2 = dp2 - __ldg(d.cp + c0 + 2 * S) * z3;
+    z1 = dp1 - __ldg(d.cp + c0 + S) * z2;
+    z0 = dp0 - __ldg(d.cp + c0) * z1;
+  } else if (upper == 3) {
+    z2 = dp2;
+    z1 = dp1 - __ldg(d.cp + c0 + S) * z2;
+    z0 = dp0 - __ldg(d.cp + c0) * z1;
+  } else if (upper == 2) {
+    z1 = dp1;
+    z0 = dp0 - __ldg(d.cp + c0) * z1;
+  } else {
+    z0 = dp0;
+  }
+  zl[0] = z0;
+  zl[1] = z1;
+  zl[2] = z2;
+  zl[3] = z3;
+}
+
+// Sum the NV tile sums of the block into per-supertile partials.
+template <int NV>
+__device__ __forceinline__ void supertile_partial(const Red& red, int s,
+                                                  const double* acc,
+                                                  double* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+#pragma unroll
+    for (int v = 0; v < NV; v++) sh[v * 8 + warp] = acc[v];
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      double t = lane < 8 ? sh[v * 8 + lane] : 0.0;
+      t = bfly(t);
+      if (lane == 0) red.partials[v * red.stride + s] = t;
+    }
+  }
+  __syncthreads();
+}
+
+// Last-block-done finish of the reduction; returns true in the block that
+// wrote the results.
+template <int NV>
+__device__ __forceinline__ bool finish_reduction(const Red& red, int ns,
+                                                 double* sh) {
+  __shared__ unsigned int is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int t = atomicAdd(red.counter, 1u);
+    is_last = (t == gridDim.x - 1) ? 1u : 0u;
+  }
+  __syncthreads();
+  if (!is_last) return false;
+  __threadfence();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll 1
+  for (int v = 0; v < NV; v++) {
+    double a = 0.0;
+    for (int k = threadIdx.x; k < ns; k += kBlock)
+      a = a + __ldcg(red.partials + v * red.stride + k);
+    a = bfly(a);
+    if (lane == 0) sh[warp] = a;
+    __syncthreads();
+    if (warp == 0) {
+      double t = lane < 8 ? sh[lane] : 0.0;
+      t = bfly(t);
+      if (lane == 0) red.result[v] = t;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *red.counter = 0u;
+  return true;
+}
+
+// Walks the block's supertiles; body(x, y0, xin, acc) processes the TH rows
+// of one lane's column x starting at interior row y0 and adds its
+// contributions row by row into acc[0..NV).  Returns true in the one block
+// that finished the reduction (thread 0 of it holds red.result).
+template <int TH, int NV, class Body>
+__device__ __forceinline__ bool tile_driver(const Dev& d, const Red& red,
+                                            Body body) {
+  __shared__ double sh[(NV > 0 ? NV : 1) * 8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int s = blockIdx.x; s < d.ns; s += gridDim.x) {
+    const int sy = s / d.nsx, sx = s - sy * d.nsx;
+    const int tx = sx * kTilesPerSuper + warp;
+    double acc[NV > 0 ? NV : 1];
+#pragma unroll
+    for (int v = 0; v < (NV > 0 ? NV : 1); v++) acc[v] = 0.0;
+    if (tx < d.ntx) {
+      const int x = tx * kTileW + lane;
+      body(x, sy * TH, x < d.x_max, acc);
+      if (NV > 0) {
+#pragma unroll
+        for (int v = 0; v < NV; v++) acc[v] = bfly(acc[v]);
+      }
+    }
+    if (NV > 0) supertile_partial<NV>(red, s, acc, sh);
+  }
+  if (NV > 0) return finish_reduction<NV>(red, d.ns, sh);
+  return false;
+}
+
+// True in the last block of the grid to get here (counter reset after).
+__device__ __forceinline__ bool last_block(unsigned int* counter) {
+  __shared__ unsigned int is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int t = atomicAdd(counter, 1u);
+    is_last = (t == gridDim.x - 1) ? 1u : 0u;
+    if (is_last) *counter = 0u;
+  }
+  __syncthreads();
+  return is_last != 0u;
+}
+
+}  // namespace tea

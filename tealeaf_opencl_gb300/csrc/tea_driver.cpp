@@ -1,0 +1,717 @@
+// Whole-run driver: a C++ restatement of the reference's Fortran caller of
+// the C ABI, so that tea.in decks run end to end on the GPU library.
+//
+//   deck reading     read_input.f90:24-329 with parse.f90's word rules
+//   problem setup    start.f90:24-115 (initialise_chunk, generate_chunk,
+//                    halo prime, set_field, first field summary)
+//   timestep loop    diffuse.f90:23-163 (constant dt, calc_dt.f90:34)
+//   implicit solve   tea_solve.f90:37-521 (tea_leaf: CG / Chebyshev / PPCG /
+//                    Jacobi, switch logic, eigenvalue estimate, PPCG inner
+//                    steps, Chebyshev first step, result check, finalise)
+//   eigen maths      tea_leaf_cheby.f90:44-172, tea_leaf_ppcg.f90:62-73
+//   summary / QA     field_summary.f90:27-110
+//
+// Every kernel is reached through the extern "C" entry points declared in
+// include/tealeaf_gb300.h, with the arguments the Fortran passes.  One chunk,
+// one tile: every neighbour is an external face.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <cctype>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/tealeaf_gb300.h"
+#include "tea_internal.h"
+
+namespace {
+
+struct State {
+  double density = 0, energy = 0, xmin = 0, xmax = 0, ymin = 0, ymax = 0,
+         radius = 0;
+  int geometry = 0;
+  bool defined = false;
+};
+
+struct Deck {
+  double xmin = 0.0, ymin = 0.0, xmax = 100.0, ymax = 100.0;
+  int x_cells = 10, y_cells = 10;
+  double end_time = 10.0;
+  int end_step = 640000;  // g_ibig
+  int summary_frequency = 10;
+  double dtinit = (double)0.1f;  // single-precision literal in read_input
+  int max_iters = 1000;
+  double eps = (double)1.0e-10f;
+  int coefficient = TEA_COEF_CONDUCTIVITY;
+  int presteps = 25;
+  double epslim = 1.0;
+  bool check_result = false;
+  int prec = TEA_PREC_NONE;
+  bool reflective = false;
+  int inner_steps = -1;
+  int solver = TEA_SOLVER_JACOBI;
+  int halo = 1;
+  int test_problem = 0;
+  bool verbose = false;
+  std::vector<State> states;
+};
+
+// parse.f90: the *tea ... *endtea block; text after '!' or ';' dropped;
+// lower case; '=' and ',' are blanks.
+std::vector<std::vector<std::string>> deck_words(const std::string& text) {
+  std::vector<std::vector<std::string>> out;
+  std::istringstream in(text);
+  std::string raw;
+  bool inside = false;
+  while (std::getline(in, raw)) {
+    for (char& ch : raw) {
+      const unsigned char u = (unsigned char)ch;
+      if (u < 32 || u > 128) ch = ' ';
+    }
+    const size_t bang = raw.find_first_of("!;");
+    if (bang != std::string::npos) raw.erase(bang);
+    for (char& ch : raw) {
+      ch = (char)std::tolower((unsigned char)ch);
+      if (ch == '=' || ch == ',') ch = ' ';
+    }
+    std::istringstream ws(raw);
+    std::vector<std::string> words;
+    std::string w;
+    while (ws >> w) words.push_back(w);
+    if (words.empty()) continue;
+    if (words[0].compare(0, 7, "*endtea") == 0) {
+      inside = false;
+      continue;
+    }
+    if (words[0].compare(0, 4, "*tea") == 0) {
+      inside = true;
+      continue;
+    }
+    if (inside) out.push_back(words);
+  }
+  return out;
+}
+
+// parse_getival: READ (I7) -- the first seven characters
+bool to_int(const std::string& s, int* v) {
+  const std::string head = s.substr(0, 7);
+  char* end = nullptr;
+  const long x = strtol(head.c_str(), &end, 10);
+  if (end == head.c_str()) return false;
+  *v = (int)x;
+  return true;
+}
+
+bool to_real(const std::string& s, double* v) {
+  char* end = nullptr;
+  const double x = strtod(s.c_str(), &end);
+  if (end == s.c_str()) return false;
+  *v = x;
+  return true;
+}
+
+bool parse_deck(const std::string& text, Deck* D, std::string* err) {
+  const auto lines = deck_words(text);
+  int nstates = 0;
+  for (const auto& L : lines) {
+    for (size_t i = 0; i < L.size(); i++) {
+      if (L[i] == "state" && i + 1 < L.size()) {
+        int s = 0;
+        if (to_int(L[i + 1], &s)) nstates = std::max(nstates, s);
+        break;
+      }
+    }
+  }
+  if (nstates < 1) {
+    *err = "read_input: No states defined.";
+    return false;
+  }
+  D->states.assign(nstates, State());
+  for (const auto& L : lines) {
+    size_t i = 0;
+    auto next = [&](void) -> std::string { return i < L.size() ? L[i++] : std::string(); };
+    bool ok = true;
+    while (i < L.size()) {
+      const std::string w = next();
+      if (w == "initial_timestep") ok = to_real(next(), &D->dtinit);
+      else if (w == "end_time") ok = to_real(next(), &D->end_time);
+      else if (w == "end_step") ok = to_int(next(), &D->end_step);
+      else if (w == "xmin") ok = to_real(next(), &D->xmin);
+      else if (w == "xmax") ok = to_real(next(), &D->xmax);
+      else if (w == "ymin") ok = to_real(next(), &D->ymin);
+      else if (w == "ymax") ok = to_real(next(), &D->ymax);
+      else if (w == "x_cells") ok = to_int(next(), &D->x_cells);
+      else if (w == "y_cells") ok = to_int(next(), &D->y_cells);
+      else if (w == "visit_frequency") { int v; ok = to_int(next(), &v); }
+      else if (w == "summary_frequency") ok = to_int(next(), &D->summary_frequency);
+      else if (w == "tl_ch_cg_presteps") ok = to_int(next(), &D->presteps);
+      else if (w == "tl_ppcg_inner_steps") ok = to_int(next(), &D->inner_steps);
+      else if (w == "tl_ch_cg_epslim") ok = to_real(next(), &D->epslim);
+      else if (w == "tl_check_result") D->check_result = true;
+      else if (w == "tl_preconditioner_type") {
+        while (i < L.size()) {
+          const std::string v = next();
+          if (v == "none") D->prec = TEA_PREC_NONE;
+          else if (v == "jac_diag") D->prec = TEA_PREC_JAC_DIAG;
+          else if (v == "jac_block") D->prec = TEA_PREC_JAC_BLOCK;
+          else {
+            *err = "read_input: Invalid preconditioner type specified: " + v;
+            return false;
+          }
+        }
+      }
+      else if (w == "verbose_on") D->verbose = true;
+      else if (w == "tl_use_jacobi") D->solver = TEA_SOLVER_JACOBI;
+      else if (w == "tl_use_cg") D->solver = TEA_SOLVER_CG;
+      else if (w == "tl_use_ppcg") D->solver = TEA_SOLVER_PPCG;
+      else if (w == "tl_use_chebyshev") D->solver = TEA_SOLVER_CHEBYSHEV;
+      else if (w == "reflective_boundary") D->reflective = true;
+      else if (w == "halo_depth") {
+        ok = to_int(next(), &D->halo);
+        if (ok && D->halo < 1) {
+          *err = "read_input: Invalid halo exchange depth specified";
+          return false;
+        }
+      }
+      else if (w == "tl_max_iters") ok = to_int(next(), &D->max_iters);
+      else if (w == "tl_eps") ok = to_real(next(), &D->eps);
+      else if (w == "tl_coefficient_density") D->coefficient = TEA_COEF_CONDUCTIVITY;
+      else if (w == "tl_coefficient_inverse_density")
+        D->coefficient = TEA_COEF_RECIP_CONDUCTIVITY;
+      else if (w == "test_problem") ok = to_int(next(), &D->test_problem);
+      else if (w == "state") {
+        int s = 0;
+        ok = to_int(next(), &s);
+        if (!ok || s < 1 || s > nstates || D->states[s - 1].defined) {
+          *err = "read_input: State defined twice.";
+          return false;
+        }
+        State& st = D->states[s - 1];
+        st.defined = true;
+        while (i < L.size() && ok) {
+          const std::string k = next();
+          if (k == "xmin") ok = to_real(next(), &st.xmin);
+          else if (k == "ymin") ok = to_real(next(), &st.ymin);
+          else if (k == "xmax") ok = to_real(next(), &st.xmax);
+          else if (k == "ymax") ok = to_real(next(), &st.ymax);
+          else if (k == "radius") ok = to_real(next(), &st.radius);
+          else if (k == "density") ok = to_real(next(), &st.density);
+          else if (k == "energy") ok = to_real(next(), &st.energy);
+          else if (k == "geometry") {
+            const std::string g = next();
+            if (g == "rectangle") st.geometry = 1;
+            else if (g == "circle") st.geometry = 2;
+            else if (g == "point") st.geometry = 3;
+          }
+        }
+      }
+      // other words (opencl_*, profiler_on, ...) are not read_input keys
+      if (!ok) {
+        *err = "parse: conversion error after '" + w + "'";
+        return false;
+      }
+    }
+  }
+  if (D->inner_steps == -1) {
+    // 4*INT(SQRT(SQRT(REAL(x_cells*y_cells)))) in default (single) precision
+    const float cells = (float)(D->x_cells * D->y_cells);
+    D->inner_steps = 4 * (int)sqrtf(sqrtf(cells));
+  }
+  const double dx = (D->xmax - D->xmin) / (double)(float)D->x_cells;
+  const double dy = (D->ymax - D->ymin) / (double)(float)D->y_cells;
+  for (size_t n = 1; n < D->states.size(); n++) {
+    State& st = D->states[n];
+    st.xmin = st.xmin + (dx / 100.0);
+    st.ymin = st.ymin + (dy / 100.0);
+    st.xmax = st.xmax - (dx / 100.0);
+    st.ymax = st.ymax - (dy / 100.0);
+  }
+  return true;
+}
+
+// tqli (tea_leaf_cheby.f90:44-94): d diagonal, e off-diagonal with e[0]
+// unused on entry (shifted down by one first, as eoshift does).
+int tqli(std::vector<double>& d, std::vector<double>& e) {
+  const int n = (int)d.size();
+  for (int i = 0; i + 1 < n; i++) e[i] = e[i + 1];
+  if (n > 0) e[n - 1] = 0.0;
+  for (int l = 0; l < n; l++) {
+    int iter = 0;
+    bool again = true;
+    while (again) {
+      int m = l;
+      while (m < n - 1) {
+        const double dd = fabs(d[m]) + fabs(d[m + 1]);
+        if (fabs(e[m]) + dd == dd) break;
+        m++;
+      }
+      if (m == l) break;
+      if (iter == 30) return 1;
+      iter++;
+      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+      double r = sqrt(g * g + 1.0);
+      g = d[m] - d[l] + e[l] / (g + copysign(fabs(r), g));
+      double s = 1.0, c = 1.0, p = 0.0;
+      bool restarted = false;
+      for (int i = m - 1; i >= l; i--) {
+        const double f = s * e[i];
+        const double b = c * e[i];
+        r = sqrt(f * f + g * g);
+        e[i + 1] = r;
+        if (r == 0.0) {
+          d[i + 1] = d[i + 1] - p;
+          e[m] = 0.0;
+          restarted = true;
+          break;
+        }
+        s = f / r;
+        c = g / r;
+        g = d[i + 1] - p;
+        r = (d[i] - g) * s + 2.0 * c * b;
+        p = s * r;
+        d[i + 1] = g + p;
+        g = c * r - b;
+      }
+      if (restarted) continue;
+      d[l] = d[l] - p;
+      e[l] = g;
+      e[m] = 0.0;
+    }
+  }
+  return 0;
+}
+
+// tea_calc_eigenvalues (tea_leaf_cheby.f90:96-143); the reference's bubble
+// sort only serves to pick the extremes.
+int calc_eigenvalues(const std::vector<double>& alphas,
+                     const std::vector<double>& betas, int nsteps,
+                     double* eigmin, double* eigmax) {
+  if (nsteps < 1) return 1;
+  std::vector<double> diag(nsteps, 0.0), off(nsteps, 0.0);
+  for (int n = 0; n < nsteps; n++) {
+    diag[n] = 1.0 / alphas[n];
+    if (n > 0) diag[n] = diag[n] + betas[n - 1] / alphas[n - 1];
+    if (n < nsteps - 1) off[n + 1] = sqrt(betas[n]) / alphas[n];
+  }
+  if (tqli(diag, off) != 0) return 1;
+  double lo = diag[0], hi = diag[0];
+  for (double v : diag) {
+    lo = std::min(lo, v);
+    hi = std::max(hi, v);
+  }
+  *eigmin = lo;
+  *eigmax = hi;
+  return (lo < 0.0 || hi < 0.0) ? 1 : 0;
+}
+
+// tea_calc_ch_coefs (tea_leaf_cheby.f90:145-172)
+void calc_ch_coefs(std::vector<double>& a, std::vector<double>& b,
+                   double eigmin, double eigmax, double* theta, int n) {
+  const double th = (eigmax + eigmin) / 2;
+  const double delta = (eigmax - eigmin) / 2;
+  const double sigma = th / delta;
+  double rho_old = 1.0 / sigma;
+  a.assign(std::max(n, 1), 0.0);
+  b.assign(std::max(n, 1), 0.0);
+  for (int i = 0; i < n; i++) {
+    const double rho_new = 1.0 / (2.0 * sigma - rho_old);
+    a[i] = rho_new * rho_old;
+    b[i] = 2.0 * rho_new / delta;
+    rho_old = rho_new;
+  }
+  *theta = th;
+}
+
+class Driver {
+ public:
+  Deck D;
+  FILE* logfile = nullptr;
+  int mode = TEA_DRIVER_PER_CALL;
+  int cap = 0;
+  bool first = true;
+  double eigmin = 0, eigmax = 0, theta = 0, cn = 0;
+  int step = 0;
+  double time = 0, dt = 0;
+  bool complete = false;
+  int neighbours[4] = {TEA_EXTERNAL_FACE, TEA_EXTERNAL_FACE, TEA_EXTERNAL_FACE,
+                       TEA_EXTERNAL_FACE};
+  tea_gb300_step_info* info = nullptr;
+
+  void say(const char* fmt, ...) {
+    if (!logfile) return;
+    va_list ap;
+    va_start(ap, fmt);
+    vfprintf(logfile, fmt, ap);
+    va_end(ap);
+  }
+
+  // update_halo.f90:30-68: the exchange is a no-op on one chunk and the
+  // boundary update only runs with reflective_boundary.
+  void update_halo(const int* fields, int depth) {
+    if (!D.reflective) return;
+    int f[7];
+    memcpy(f, fields, sizeof(f));
+    update_halo_kernel_ocl_(neighbours, f, &depth);
+  }
+
+  void field_summary() {
+    double vol, mass, ie, temp;
+    field_summary_kernel_ocl_(&vol, &mass, &ie, &temp);
+    say("\n Time %.15g\n", time);
+    say(" step:%7d%26.17E%26.17E%26.17E%26.17E%26.17E\n", step, vol, mass,
+         mass / vol, ie, temp);
+    if (info) {
+      info->summary_done = 1;
+      info->vol = vol;
+      info->mass = mass;
+      info->ie = ie;
+      info->temp = temp;
+    }
+    if (complete && D.test_problem >= 1 && D.test_problem <= 6) {
+      static const double golden[7] = {0.0, 157.550841832793, 116.067951160930,
+                                       95.4865103390698, 166.838315378708,
+                                       116.482111627676, 103.88639125996923};
+      const double qa = fabs((100.0 * (temp / golden[D.test_problem])) - 100.0);
+      say("Test problem %4d is within %16.7E%% of the expected solution\n",
+           D.test_problem, qa);
+      say(" %s\n", qa < 0.001 ? "This test is considered PASSED"
+                               : "This test is considered NOT PASSED");
+      if (info) {
+        info->qa_passed = qa < 0.001 ? 1 : 0;
+        info->qa_diff = qa;
+      }
+    }
+  }
+
+  bool open(const std::string& text, const char* log_path, int m, int c,
+            std::string* err) {
+    if (!parse_deck(text, &D, err)) return false;
+    if (D.halo > 1 && D.prec == TEA_PREC_JAC_BLOCK &&
+        D.solver == TEA_SOLVER_PPCG) {
+      // read_input.f90:299-301 rejects this combination because of its
+      // multi-chunk matrix-powers bounds; on one chunk the halo depth does
+      // not change the arithmetic, so it is accepted here.
+    }
+    mode = m;
+    cap = c;
+    if (log_path) logfile = fopen(log_path, "w");
+    if (tea_gb300_configure(D.halo, D.solver, D.prec, 0) != 0) {
+      *err = "invalid configuration";
+      return false;
+    }
+    int x0 = 1, y0 = 1;
+    initialise_ocl_(&x0, &D.x_cells, &y0, &D.y_cells);
+    if (tea::error_code() != 0) {
+      *err = "initialise_ocl_ failed";
+      return false;
+    }
+    time = 0.0;
+    step = 0;
+    dt = D.dtinit;
+    double dx = (D.xmax - D.xmin) / (double)(float)D.x_cells;
+    double dy = (D.ymax - D.ymin) / (double)(float)D.y_cells;
+    double xmin = D.xmin + dx * 0.0, ymin = D.ymin + dy * 0.0;
+    initialise_chunk_kernel_ocl_(&xmin, &ymin, &dx, &dy);
+    const int ns = (int)D.states.size();
+    std::vector<double> sd(ns), se(ns), sx0(ns), sx1(ns), sy0(ns), sy1(ns),
+        srad(ns);
+    std::vector<int> sg(ns);
+    for (int s = 0; s < ns; s++) {
+      sd[s] = D.states[s].density;
+      se[s] = D.states[s].energy;
+      sx0[s] = D.states[s].xmin;
+      sx1[s] = D.states[s].xmax;
+      sy0[s] = D.states[s].ymin;
+      sy1[s] = D.states[s].ymax;
+      srad[s] = D.states[s].radius;
+      sg[s] = D.states[s].geometry;
+    }
+    const int g_rect = 1, g_circ = 2, g_point = 3;
+    generate_chunk_kernel_ocl_(&ns, sd.data(), se.data(), sx0.data(),
+                               sx1.data(), sy0.data(), sy1.data(), srad.data(),
+                               sg.data(), &g_rect, &g_circ, &g_point);
+    const int prime[7] = {1, 1, 1, 0, 0, 0, 0};
+    update_halo(prime, D.halo);
+    set_field_kernel_ocl_();
+    field_summary();
+    return tea::error_code() == 0;
+  }
+
+  // tea_leaf_run_ppcg_inner_steps, tea_solve.f90:422-475
+  void ppcg_inner_steps() {
+    const int fu[7] = {0, 0, 0, 1, 0, 0, 0};
+    update_halo(fu, 1);
+    tea_leaf_ppcg_init_sd_kernel_ocl_();
+    for (int cur = 1; cur <= D.inner_steps; cur += D.halo) {
+      const int fsr[7] = {0, 0, 0, 0, 0, 1, 1};
+      update_halo(fsr, D.halo);
+      int inner_step = cur;
+      for (int bounds_extra = D.halo - 1; bounds_extra >= 0; bounds_extra--) {
+        tea_leaf_ppcg_inner_kernel_ocl_(&inner_step, &bounds_extra, neighbours);
+        inner_step++;
+        if (inner_step > D.inner_steps) break;
+      }
+    }
+  }
+
+  // SUBROUTINE tea_leaf (tea_solve.f90:37-420)
+  int tea_leaf() {
+    const int max_iters = D.max_iters;
+    const bool use_cg = D.solver == TEA_SOLVER_CG;
+    const bool use_cheby = D.solver == TEA_SOLVER_CHEBYSHEV;
+    const bool use_ppcg = D.solver == TEA_SOLVER_PPCG;
+    const bool use_jacobi = D.solver == TEA_SOLVER_JACOBI;
+    const int loop_max = (cap > 0 && cap < max_iters) ? cap : max_iters;
+
+    std::vector<double> cg_alphas(max_iters + 2, 0.0), cg_betas(max_iters + 2, 0.0);
+    std::vector<double> ch_alphas, ch_betas;
+    int cheby_calc_steps = 0, ppcg_inner_iters = 0, est_itc = 0,
+        max_cheby_iters = 0;
+    bool ch_switch_check = false;
+    double rro = 0, pw = 0, rrn = 0, alpha, beta;
+    double old_error, error = 0.0, exact_error = 0.0, initial_residual;
+
+    const int f_de[7] = {1, 0, 1, 0, 0, 0, 0};
+    update_halo(f_de, D.halo);
+    int zero_boundary[4] = {1, 1, 1, 1};
+    int reflective = D.reflective ? 1 : 0;
+    double rx, ry;
+    tea_leaf_common_init_kernel_ocl_(&D.coefficient, &dt, &rx, &ry,
+                                     zero_boundary, &reflective);
+    const int fu[7] = {0, 0, 0, 1, 0, 0, 0};
+    update_halo(fu, 1);
+    tea_leaf_calc_residual_ocl_();
+    int which = 1;
+    tea_leaf_calc_2norm_kernel_ocl_(&which, &initial_residual);
+    old_error = initial_residual;
+    initial_residual = sqrt(initial_residual);
+    if (D.verbose) say(" Initial residual %.17E\n", initial_residual);
+
+    if (use_cg || use_cheby || use_ppcg) tea_leaf_cg_init_kernel_ocl_(&rro);
+
+    int n = 1;
+    bool exited = false;
+    while (n <= loop_max) {
+      if (!ch_switch_check) {
+        if (cheby_calc_steps > 0)
+          ch_switch_check = true;
+        else if (!first && use_ppcg && n > 1)
+          ch_switch_check = true;
+        else if (fabs(old_error) <= D.epslim && n >= D.presteps)
+          ch_switch_check = true;
+        else
+          ch_switch_check = false;
+      }
+
+      if ((use_cheby || use_ppcg) && ch_switch_check) {
+        if (cheby_calc_steps == 0) {
+          max_cheby_iters = max_iters - n + 2;
+          if (first) {
+            const std::vector<double> a(cg_alphas.begin() + 1, cg_alphas.end());
+            const std::vector<double> b(cg_betas.begin() + 1, cg_betas.end());
+            const int info_e = calc_eigenvalues(a, b, n - 1, &eigmin, &eigmax);
+            first = false;
+            if (info_e != 0) {
+              tea::fail(20, "tea_leaf: Error in calculating eigenvalues");
+              return -1;
+            }
+            eigmin = eigmin * 0.95;
+            eigmax = eigmax * 1.05;
+          }
+          if (use_cheby)
+            calc_ch_coefs(ch_alphas, ch_betas, eigmin, eigmax, &theta,
+                          max_cheby_iters);
+          else
+            calc_ch_coefs(ch_alphas, ch_betas, eigmin, eigmax, &theta,
+                          D.inner_steps);
+          cn = eigmax / eigmin;
+          say("Switching after %3d CG its, error %15.7E\n", n, rro);
+          say("Eigen min%14.6E Eigen max%14.6E Condition number%14.6f "
+               "Error%14.6E\n",
+               eigmin, eigmax, cn, old_error);
+        }
+        if (use_cheby) {
+          if (cheby_calc_steps == 0) {
+            // tea_leaf_cheby_first_step (tea_solve.f90:477-521); its error
+            // argument is the caller's old_error
+            double bb;
+            int w0 = 0, w1 = 1, one = 1;
+            tea_leaf_calc_2norm_kernel_ocl_(&w0, &bb);
+            tea_leaf_cheby_init_kernel_ocl_(ch_alphas.data(), ch_betas.data(),
+                                            &max_cheby_iters, &rx, &ry, &theta);
+            update_halo(fu, 1);
+            tea_leaf_cheby_iterate_kernel_ocl_(&one);
+            tea_leaf_calc_2norm_kernel_ocl_(&w1, &old_error);
+            const double it_alpha = D.eps * bb / (4.0 * old_error);
+            const double gamm = (sqrt(cn) - 1.0) / (sqrt(cn) + 1.0);
+            const double q = log(it_alpha) / (2.0 * log(gamm));
+            est_itc = std::isfinite(q) ? (int)lround(q) : 0;
+            say("est itc\n%11d\n", est_itc);
+            cheby_calc_steps = 1;
+          } else {
+            tea_leaf_cheby_iterate_kernel_ocl_(&cheby_calc_steps);
+            if (n >= est_itc && n % 10 == 0) {
+              int w1 = 1;
+              tea_leaf_calc_2norm_kernel_ocl_(&w1, &error);
+            }
+          }
+        } else {
+          if (cheby_calc_steps == 0)
+            tea_leaf_ppcg_init_ocl_(ch_alphas.data(), ch_betas.data(), &theta,
+                                    &D.inner_steps);
+          tea_leaf_cg_calc_w_kernel_ocl_(&pw);
+          alpha = rro / pw;
+          tea_leaf_cg_calc_ur_kernel_ocl_(&alpha, &rrn);
+          ppcg_inner_steps();
+          ppcg_inner_iters += D.inner_steps;
+          int w2 = 2;
+          tea_leaf_calc_2norm_kernel_ocl_(&w2, &rrn);
+          beta = rrn / rro;
+          tea_leaf_cg_calc_p_kernel_ocl_(&beta);
+          error = rrn;
+          rro = rrn;
+        }
+        cheby_calc_steps++;
+      } else if (use_cg || use_cheby || use_ppcg) {
+        if (mode == TEA_DRIVER_RESIDENT && use_cg) {
+          // The whole remaining CG loop runs on the device; it stops exactly
+          // where this loop would (same tests, same arithmetic).
+          int n_done = 0, conv = 0;
+          if (tea::resident_cg_iterations(n, loop_max, rro,
+                                          D.eps * initial_residual, &rro,
+                                          &error, &n_done, &conv,
+                                          cg_alphas.data(), cg_betas.data()) != 0)
+            return -1;
+          n = n_done;
+          if (conv) {
+            exited = true;
+            break;
+          }
+          n++;
+          continue;
+        }
+        tea_leaf_cg_calc_w_kernel_ocl_(&pw);
+        alpha = rro / pw;
+        cg_alphas[n] = alpha;
+        tea_leaf_cg_calc_ur_kernel_ocl_(&alpha, &rrn);
+        beta = rrn / rro;
+        cg_betas[n] = beta;
+        tea_leaf_cg_calc_p_kernel_ocl_(&beta);
+        error = rrn;
+        rro = rrn;
+      } else if (use_jacobi) {
+        tea_leaf_jacobi_solve_kernel_ocl_(&error);
+      }
+
+      update_halo(fu, 1);
+      error = sqrt(error);
+      if (D.verbose) say(" Residual %.17E\n", error);
+      if (fabs(error) < D.eps * initial_residual) {
+        exited = true;
+        break;
+      }
+      old_error = error;
+      n++;
+    }
+    const int performed = exited ? n : loop_max;
+
+    if (D.check_result) {
+      update_halo(fu, 1);
+      tea_leaf_calc_residual_ocl_();
+      int w1 = 1;
+      tea_leaf_calc_2norm_kernel_ocl_(&w1, &exact_error);
+      exact_error = sqrt(exact_error);
+    }
+    say("Conduction error %14.7E\n", error / initial_residual);
+    if (D.check_result)
+      say("EXACT error calculated as%14.7E\n", exact_error / initial_residual);
+    say("Iteration count %8d\n", performed - (exited ? 1 : 0));
+    if (use_ppcg)
+      say("PPCG Iteration count%8d (Total %8d)\n", ppcg_inner_iters,
+           ppcg_inner_iters + performed - (exited ? 1 : 0));
+
+    tea_leaf_common_finalise_kernel_ocl_();
+    const int fe[7] = {0, 0, 1, 0, 0, 0, 0};
+    update_halo(fe, 1);
+
+    if (info) {
+      info->iterations = performed;
+      info->inner_iterations = ppcg_inner_iters;
+      info->conduction_error = error / initial_residual;
+      info->exact_error = D.check_result ? exact_error / initial_residual : NAN;
+    }
+    return tea::error_code() == 0 ? 0 : -1;
+  }
+
+  // one pass of the diffuse loop (diffuse.f90:43-90)
+  int do_step(tea_gb300_step_info* out) {
+    if (complete) return 1;
+    tea_gb300_step_info local;
+    memset(&local, 0, sizeof(local));
+    local.qa_passed = -1;
+    local.exact_error = NAN;
+    info = &local;
+    step++;
+    if (D.dtinit <= dt) dt = D.dtinit;  // timestep.f90 with calc_dt = dtinit
+    say(" Step %7d time %11.7f timestep  %9.2E\n", step, time, dt);
+    const int rc = tea_leaf();
+    if (rc != 0) {
+      info = nullptr;
+      return -1;
+    }
+    time = time + dt;
+    if (D.summary_frequency != 0 && step % D.summary_frequency == 0)
+      field_summary();
+    const double g_small = (double)1.0e-16f;
+    if (time + g_small > D.end_time || step >= D.end_step) {
+      complete = true;
+      field_summary();
+    }
+    local.step = step;
+    local.time = time;
+    local.dt = dt;
+    local.complete = complete ? 1 : 0;
+    if (out) *out = local;
+    info = nullptr;
+    return 0;
+  }
+};
+
+Driver* g_driver = nullptr;
+
+}  // namespace
+
+extern "C" int tea_gb300_driver_open(const char* deck_text,
+                                     const char* log_path, int mode,
+                                     int max_iters_cap) {
+  delete g_driver;
+  g_driver = new Driver();
+  std::string err;
+  if (mode != TEA_DRIVER_PER_CALL && mode != TEA_DRIVER_RESIDENT) {
+    tea::fail(21, "unknown driver mode %d", mode);
+    return -1;
+  }
+  if (!g_driver->open(deck_text ? deck_text : "", log_path, mode,
+                      max_iters_cap, &err)) {
+    if (!err.empty()) tea::fail(22, "%s", err.c_str());
+    return -1;
+  }
+  return 0;
+}
+
+extern "C" int tea_gb300_driver_step(tea_gb300_step_info* info) {
+  if (!g_driver) {
+    tea::fail(23, "tea_gb300_driver_step before tea_gb300_driver_open");
+    return -1;
+  }
+  return g_driver->do_step(info);
+}
+
+extern "C" void tea_gb300_driver_close(void) {
+  if (g_driver && g_driver->logfile) fclose(g_driver->logfile);
+  delete g_driver;
+  g_driver = nullptr;
+}

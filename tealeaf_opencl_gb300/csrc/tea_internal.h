@@ -1,0 +1,169 @@
+// Internal declarations shared by the CUDA kernels, the C-ABI layer and the
+// resident solver of libtealeaf_gb300.so.
+//
+// Field layout in HBM.  Every 2-D field is FP64, x fastest.  Padded
+// coordinates (col,row) follow the reference (interior at
+// [H, H+x_max) x [H, H+y_max), halo of depth H around it;
+// THARR2D, macros_cl.cl:20-22) but the row stride S is rounded up to a
+// multiple of 32 doubles (256 B) and the base is offset so that interior
+// column H of every row starts on a 256-byte boundary.  Each field holds
+// y_max+2H+1 rows of S doubles (the extra row and the columns past x_max+2H
+// play the role of the reference's "+1" allocations, ocl_buffers.cpp:55-69)
+// and is zero-filled at allocation, as the reference's buffers are.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+namespace tea {
+
+constexpr int kBlock = 256;  // threads per block of every tile kernel
+constexpr int kTileW = 32;   // columns per tile (one per lane)
+constexpr int kTilesPerSuper = 8;  // tiles per supertile (one per warp)
+
+enum Prec { PREC_NONE = 1, PREC_JAC_DIAG = 2, PREC_JAC_BLOCK = 3 };
+enum Solver { SOLVER_JACOBI = 1, SOLVER_CG = 2, SOLVER_CHEBY = 3, SOLVER_PPCG = 4 };
+
+// POD view of the chunk passed by value to every kernel.
+struct Dev {
+  int x_max, y_max, H;
+  long long S;        // row stride in doubles
+  int xs, ys;         // logical padded extents x_max+2H, y_max+2H
+  int prec;
+  int block_top_check;  // y_max % 4 != 0 (ocl_kernels.cpp:26-29)
+  int ntx, nsx, nty, ns;  // tiling for the chunk's tile height
+  double *density, *energy0, *energy1, *volume;
+  double *u, *u0, *p, *r, *w, *Mi, *Kx, *Ky, *sd, *z, *cp, *bfp, *un;
+  double *cellx, *celly, *celldx, *celldy, *vertexx, *vertexy, *vertexdx,
+      *vertexdy;
+};
+
+// Scratch for the fixed-order reductions: per-supertile partial sums, a
+// completion counter and the reduced values.
+struct Red {
+  double* partials;     // [nvals][stride]
+  long long stride;     // >= number of supertiles
+  unsigned int* counter;
+  double* result;       // [nvals]
+};
+
+// Scalar state of the device-resident CG loop: the host scalars of
+// tea_solve.f90:270-300 kept in device memory.
+struct ResState {
+  double rro, pw, rrn, alpha, beta, error;
+  double eps_target;  // eps * initial_residual
+  int n, loop_max;
+  int stop;       // set when the loop has converged or reached loop_max
+  int p_pending;  // calc_p of the current iteration still to run
+  int converged;
+  int pad;
+  double* alphas;  // indexed by iteration number n
+  double* betas;
+};
+
+struct Field {
+  double* base = nullptr;  // cudaMalloc'd allocation
+  double* f = nullptr;     // element (0,0) of the padded layout
+};
+
+// Host-side chunk state (one per process, as CloverChunk in the reference).
+struct Chunk {
+  bool ready = false;
+  int x_max = 0, y_max = 0, H = 1;
+  int solver = SOLVER_JACOBI, prec = PREC_NONE;
+  bool profiler_on = false;
+  int TH = 4;  // reduction tile height
+  long long S = 0;
+  long long rows = 0;
+  size_t field_doubles = 0;
+  int device = 0, num_sms = 0;
+  cudaStream_t stream = nullptr;
+  Field density, energy0, energy1, volume, u, u0, p, r, w, Mi, Kx, Ky, sd, z,
+      cp, bfp, un;
+  double *cellx = nullptr, *celly = nullptr, *celldx = nullptr,
+         *celldy = nullptr, *vertexx = nullptr, *vertexy = nullptr,
+         *vertexdx = nullptr, *vertexdy = nullptr;
+  // reductions
+  double* red_partials = nullptr;
+  long long red_stride = 0;
+  unsigned int* red_counter = nullptr;
+  double* red_result = nullptr;
+  double* host_result = nullptr;  // pinned, 8 doubles
+  // coefficients kept on the host (passed to kernels by value) and on device
+  double* cheby_alpha_h = nullptr;
+  double* cheby_beta_h = nullptr;
+  int n_cheby = 0;
+  double cheby_theta = 0.0;
+  double* ppcg_alpha_h = nullptr;
+  double* ppcg_beta_h = nullptr;
+  int n_ppcg = 0;
+  double ppcg_theta = 0.0;
+  double celldx_h = 0.0, celldy_h = 0.0;
+  // device-resident CG loop
+  ResState* res_state = nullptr;       // device
+  ResState* res_state_h = nullptr;     // pinned mirror
+  double* res_coef = nullptr;          // device alphas/betas
+  int res_coef_n = 0;
+  unsigned int* res_counter = nullptr;
+  cudaGraphExec_t res_graph = nullptr;
+  int res_graph_iters = 0;
+
+  Dev dev() const;
+  Red red() const;
+};
+
+Chunk& chunk();
+
+// error handling (tea_abi.cu)
+void fail(int code, const char* fmt, ...);
+int error_code();
+bool check_cuda(cudaError_t e, const char* what);
+void count_launch(const char* name);
+void profile_begin(const char* name);
+void profile_end(const char* name);
+
+int reduction_rows(int x_max, int y_max);
+
+// ---- kernel launch wrappers (tea_kernels.cu) ----
+// setup
+void launch_initialise_chunk(Chunk& c, double xmin, double ymin, double dx,
+                             double dy);
+void launch_generate_init(Chunk& c, double density0, double energy0);
+void launch_generate_state(Chunk& c, double density, double energy,
+                           double xmin, double xmax, double ymin, double ymax,
+                           double radius, int geometry, int g_rect, int g_circ,
+                           int g_point);
+void launch_init_u(Chunk& c, const double* energy);
+void launch_set_field(Chunk& c);
+// solver
+void launch_init_common(Chunk& c, int coef, double rx, double ry);
+void launch_zero_boundary(Chunk& c, const int* zero_boundary);
+void launch_calc_residual(Chunk& c);
+void launch_dot(Chunk& c, const double* a, const double* b);
+void launch_init_jac_diag(Chunk& c);
+void launch_block_init(Chunk& c);
+void launch_cg_init_p(Chunk& c);
+void launch_cg_calc_w(Chunk& c);
+void launch_cg_calc_ur(Chunk& c, double alpha);
+void launch_cg_calc_p(Chunk& c, double beta);
+void launch_cheby_init_p(Chunk& c, double theta);
+void launch_cheby_calc_p(Chunk& c, double alpha, double beta);
+void launch_cheby_calc_u(Chunk& c);
+void launch_ppcg_init_sd(Chunk& c, double theta);
+void launch_ppcg_update_r(Chunk& c);
+void launch_ppcg_calc_sd(Chunk& c, double alpha, double beta);
+void launch_jacobi_copy_u(Chunk& c);
+void launch_jacobi_solve(Chunk& c);
+void launch_finalise(Chunk& c);
+void launch_field_summary(Chunk& c);
+void launch_update_halo(Chunk& c, int mask, int depth);
+// device-resident CG loop (tea_kernels.cu)
+int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
+                           double eps_target, double* rro_out,
+                           double* error_out, int* n_done, int* converged,
+                           double* cg_alphas, double* cg_betas);
+void resident_release();
+
+}  // namespace tea

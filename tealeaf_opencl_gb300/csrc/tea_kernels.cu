@@ -1,0 +1,1018 @@
+// CUDA kernels of the per-call C ABI, one per reference kernel (or fused
+// pair), each citing the OpenCL kernel whose arithmetic it reproduces.
+// Interior kernels use the tile walk of tea_device.cuh; setup and
+// whole-array kernels use plain 2-D grids.
+#include <algorithm>
+#include <unordered_map>
+
+#include "tea_device.cuh"
+
+namespace tea {
+
+// ---------------------------------------------------------------------------
+// launch helpers
+// ---------------------------------------------------------------------------
+
+static int blocks_per_sm(const void* fn) {
+  static std::unordered_map<const void*, int> cache;
+  auto it = cache.find(fn);
+  if (it != cache.end()) return it->second;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kBlock, 0) !=
+          cudaSuccess ||
+      n < 1)
+    n = 1;
+  cache[fn] = n;
+  return n;
+}
+
+template <class... KArgs, class... Args>
+static void launch_tile(Chunk& c, const char* name, void (*kernel)(KArgs...),
+                        Args... args) {
+  const Dev d = c.dev();
+  const long long cap = (long long)c.num_sms * blocks_per_sm((const void*)kernel);
+  const int grid = (int)std::max<long long>(1, std::min<long long>(d.ns, cap));
+  profile_begin(name);
+  kernel<<<grid, kBlock, 0, c.stream>>>(args...);
+  count_launch(name);
+  check_cuda(cudaGetLastError(), name);
+  profile_end(name);
+}
+
+template <class... KArgs, class... Args>
+static void launch_2d(Chunk& c, const char* name, int nx, int ny,
+                      void (*kernel)(KArgs...), Args... args) {
+  if (nx <= 0 || ny <= 0) return;
+  const dim3 block(32, 8);
+  const dim3 grid((nx + 31) / 32, (ny + 7) / 8);
+  profile_begin(name);
+  kernel<<<grid, block, 0, c.stream>>>(args...);
+  count_launch(name);
+  check_cuda(cudaGetLastError(), name);
+  profile_end(name);
+}
+
+#define TH_DISPATCH(c, name, kern, ...)                   \
+  do {                                                    \
+    if ((c).TH == 16)                                     \
+      launch_tile(c, name, kern<16>, __VA_ARGS__);        \
+    else                                                  \
+      launch_tile(c, name, kern<4>, __VA_ARGS__);         \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// setup kernels
+// ---------------------------------------------------------------------------
+
+// initialise_chunk_first, initialise_chunk_cl.cl:3-49 (1-D arrays)
+__global__ void k_init_chunk_1d(Dev d, double xmin, double ymin, double dx,
+                                double dy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int H = d.H;
+  if (i <= d.x_max + H) {
+    d.vertexx[i] = xmin + dx * (double)(((i)-1) - H + 1);
+    d.vertexdx[i] = dx;
+    const double plus1 = xmin + dx * (double)((i)-H + 1);
+    d.cellx[i] = 0.5 * (d.vertexx[i] + plus1);
+    d.celldx[i] = dx;
+  }
+  if (i <= d.y_max + H) {
+    d.vertexy[i] = ymin + dy * (double)(((i)-1) - H + 1);
+    d.vertexdy[i] = dy;
+    const double plus1 = ymin + dy * (double)((i)-H + 1);
+    d.celly[i] = 0.5 * (d.vertexy[i] + plus1);
+    d.celldy[i] = dy;
+  }
+}
+
+// initialise_chunk_second, initialise_chunk_cl.cl:51-68 (volume only; no
+// kernel of the solve reads xarea/yarea)
+__global__ void k_volume(Dev d, double vol) {
+  const int col = d.H - 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = d.H - 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (col <= d.x_max + d.H && row <= d.y_max + d.H)
+    d.volume[(long long)row * d.S + col] = vol;
+}
+
+// generate_chunk_init, generate_chunk_cl.cl:82-95
+__global__ void k_gen_init(Dev d, double dens0, double en0) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x < d.x_max && y < d.y_max) {
+    const long long c = cidx(d, x, y);
+    d.energy0[c] = en0;
+    d.density[c] = dens0;
+  }
+}
+
+// generate_chunk, generate_chunk_cl.cl:3-65, one state
+__global__ void k_gen_state(Dev d, double dens, double en, double sxmin,
+                            double sxmax, double symin, double symax,
+                            double srad, int geom, int g_rect, int g_circ,
+                            int g_point) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= d.x_max || y >= d.y_max) return;
+  const int col = x + d.H, row = y + d.H;
+  const double x_cent = sxmin, y_cent = symin;
+  bool hit = false;
+  if (g_rect == geom) {
+    hit = d.vertexx[1 + col] >= sxmin && d.vertexx[col] < sxmax &&
+          d.vertexy[1 + row] >= symin && d.vertexy[row] < symax;
+  } else if (geom == g_circ) {
+    const double x_pos = d.cellx[col] - x_cent;
+    const double y_pos = d.celly[row] - y_cent;
+    const double radius = sqrt(x_pos * x_pos + y_pos * y_pos);
+    hit = radius <= srad;
+  } else if (geom == g_point) {
+    hit = d.vertexx[col] == x_cent && d.vertexy[row] == y_cent;
+  }
+  if (hit) {
+    const long long c = cidx(d, x, y);
+    d.energy0[c] = en;
+    d.density[c] = dens;
+  }
+}
+
+// generate_chunk_init_u, generate_chunk_cl.cl:67-80
+__global__ void k_init_u(Dev d, const double* __restrict__ energy) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x < d.x_max && y < d.y_max) {
+    const long long c = cidx(d, x, y);
+    d.u[c] = energy[c] * d.density[c];
+    d.u0[c] = energy[c] * d.density[c];
+  }
+}
+
+// set_field, set_field_cl.cl:3-13
+__global__ void k_set_field(Dev d) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x < d.x_max && y < d.y_max) {
+    const long long c = cidx(d, x, y);
+    d.energy1[c] = d.energy0[c];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// whole-array solver kernels
+// ---------------------------------------------------------------------------
+
+// tea_leaf_init_common, tea_leaf_common_cl.cl:56-90, over
+// [1, x_max+2H) x [1, y_max+2H)
+__global__ void k_init_common(Dev d, int coef, double rx, double ry) {
+  const int col = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (col >= d.xs || row >= d.ys) return;
+  const long long c = (long long)row * d.S + col;
+  double dc = 0.0, dl = 0.0, dd = 0.0;
+  if (coef == 1) {
+    dc = d.density[c];
+    dl = d.density[c - 1];
+    dd = d.density[c - d.S];
+  } else if (coef == 2) {
+    dc = 1.0 / d.density[c];
+    dl = 1.0 / d.density[c - 1];
+    dd = 1.0 / d.density[c - d.S];
+  }
+  double kx = (dl + dc) / (2.0 * dl * dc);
+  kx = kx * rx;
+  double ky = (dd + dc) / (2.0 * dd * dc);
+  ky = ky * ry;
+  d.Kx[c] = kx;
+  d.Ky[c] = ky;
+}
+
+// tea_leaf_zero_boundary, tea_leaf_common_cl.cl:92-125, whole padded array
+__global__ void k_zero_boundary(Dev d, int zl, int zr, int zb, int zt) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = blockIdx.y * blockDim.y + threadIdx.y;
+  if (col >= d.xs || row >= d.ys) return;
+  const long long c = (long long)row * d.S + col;
+  const int H = d.H;
+  if (zl && col <= H) {
+    d.Kx[c] = 0;
+    if (col < H) d.Ky[c] = 0;
+  }
+  if (zr && col > (d.x_max - 1) + H) {
+    d.Kx[c] = 0;
+    d.Ky[c] = 0;
+  }
+  if (zb && row <= H) {
+    d.Ky[c] = 0;
+    if (row < H) d.Kx[c] = 0;
+  }
+  if (zt && row > (d.y_max - 1) + H) {
+    d.Ky[c] = 0;
+    d.Kx[c] = 0;
+  }
+}
+
+// tea_leaf_init_jac_diag, tea_leaf_common_cl.cl:127-142, whole padded array
+__global__ void k_init_jac_diag(Dev d) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = blockIdx.y * blockDim.y + threadIdx.y;
+  if (col >= d.xs || row >= d.ys) return;
+  const long long c = (long long)row * d.S + col;
+  const double diag = (1.0 + (d.Ky[c + d.S] + d.Ky[c]) + (d.Kx[c + 1] + d.Kx[c]));
+  d.Mi[c] = 1.0 / diag;
+}
+
+// tea_leaf_block_init, tea_block_jacobi.cl:78-105: one thread per column of
+// one 4-row strip
+__global__ void k_block_init(Dev d) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int g = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= d.x_max || 4 * g >= d.y_max) return;
+  const int upper = strip_rows(d, 4 * g);
+  const long long S = d.S;
+  const long long c0 = cidx(d, x, 4 * g);
+  double cpv = (-d.Ky[c0 + S]) / coef_b(d, c0);
+  d.cp[c0] = cpv;
+  for (int k = 1; k < upper; k++) {
+    const long long ck = c0 + k * S;
+    const double b = 1.0 / (coef_b(d, ck) - (-d.Ky[ck]) * cpv);
+    d.bfp[ck] = b;
+    cpv = (-d.Ky[ck + S]) * b;
+    d.cp[ck] = cpv;
+  }
+}
+
+// update_halo_{bottom,top,left,right} (update_halo_cl.cl:3-69) fused: every
+// cell of the depth-wide ring takes the value of its mirror image in the
+// interior; corners mirror in both directions, which is what the
+// reference's bottom/top-then-left/right order produces.  Sources are
+// interior cells only, so the single pass has no hazards.
+__global__ void k_update_halo(Dev d, int mask, int depth) {
+  const int H = d.H;
+  const int col = H - depth + blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = H - depth + blockIdx.y * blockDim.y + threadIdx.y;
+  const int ce = d.x_max + H, re = d.y_max + H;
+  if (col >= ce + depth || row >= re + depth) return;
+  const bool cin = col >= H && col < ce, rin = row >= H && row < re;
+  if (cin && rin) return;
+  const int mc = col < H ? 2 * H - 1 - col : (col >= ce ? 2 * ce - 1 - col : col);
+  const int mr = row < H ? 2 * H - 1 - row : (row >= re ? 2 * re - 1 - row : row);
+  const long long dst = (long long)row * d.S + col;
+  const long long src = (long long)mr * d.S + mc;
+  if (mask & 1) d.density[dst] = d.density[src];
+  if (mask & 2) d.energy0[dst] = d.energy0[src];
+  if (mask & 4) d.energy1[dst] = d.energy1[src];
+}
+
+// ---------------------------------------------------------------------------
+// interior tile kernels
+// ---------------------------------------------------------------------------
+
+// tea_leaf_calc_residual, tea_leaf_common_cl.cl:17-36
+template <int TH>
+__global__ void __launch_bounds__(kBlock) k_calc_residual(Dev d, Red red) {
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      if (y < d.y_max) {
+        const long long c = cidx(d, x, y);
+        const double s = smvp(d, d.u, c);
+        d.r[c] = d.u0[c] - s;
+      }
+    }
+  });
+}
+
+// tea_leaf_calc_2norm, tea_leaf_common_cl.cl:38-54
+template <int TH>
+__global__ void __launch_bounds__(kBlock)
+    k_dot(Dev d, Red red, const double* a, const double* b) {
+  tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      double v = 0.0;
+      if (xin && y < d.y_max) {
+        const long long c = cidx(d, x, y);
+        v = a[c] * b[c];
+      }
+      acc[0] = acc[0] + v;
+    }
+  });
+}
+
+// tea_leaf_block_solve (tea_block_jacobi.cl:44-76) fused with
+// tea_leaf_cg_solve_init_p (tea_leaf_cg_cl.cl:8-41): z = M^-1 r, p = z,
+// sum r.p
+template <int TH>
+__global__ void __launch_bounds__(kBlock) k_cg_init_p(Dev d, Red red) {
+  tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (d.prec == PREC_JAC_BLOCK) {
+#pragma unroll 1
+      for (int ys = y0; ys < y0 + TH; ys += 4) {
+        double zl[4] = {0.0, 0.0, 0.0, 0.0}, rl[4];
+        const long long c0 = cidx(d, x, ys);
+        if (xin && ys < d.y_max) {
+#pragma unroll
+          for (int i = 0; i < 4; i++)
+            rl[i] = (ys + i < d.y_max) ? d.r[c0 + i * d.S] : 0.0;
+          strip_solve(d, c0, strip_rows(d, ys), rl, zl);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          double v = 0.0;
+          if (xin && ys + i < d.y_max) {
+            const long long c = c0 + i * d.S;
+            d.z[c] = zl[i];
+            d.p[c] = zl[i];
+            v = rl[i] * zl[i];
+          }
+          acc[0] = acc[0] + v;
+        }
+      }
+    } else {
+#pragma unroll 4
+      for (int j = 0; j < TH; j++) {
+        const int y = y0 + j;
+        double v = 0.0;
+        if (xin && y < d.y_max) {
+          const long long c = cidx(d, x, y);
+          const double rv = d.r[c];
+          double pv;
+          if (d.prec == PREC_JAC_DIAG) {
+            pv = rv * d.Mi[c];
+            d.z[c] = pv;
+          } else {
+            pv = rv;
+          }
+          d.p[c] = pv;
+          v = rv * pv;
+        }
+        acc[0] = acc[0] + v;
+      }
+    }
+  });
+}
+
+// tea_leaf_cg_solve_calc_w, tea_leaf_cg_cl.cl:45-69.  With st != nullptr
+// (device-resident loop) it does nothing once the loop has stopped and
+// leaves pw in st.
+template <int TH>
+__global__ void __launch_bounds__(kBlock)
+    k_cg_calc_w(Dev d, Red red, ResState* st) {
+  if (st && *(volatile int*)&st->stop) return;
+  const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      double v = 0.0;
+      if (xin && y < d.y_max) {
+        const long long c = cidx(d, x, y);
+        const double wv = smvp(d, d.p, c);
+        d.w[c] = wv;
+        v = d.p[c] * wv;
+      }
+      acc[0] = acc[0] + v;
+    }
+  });
+  if (st && last && threadIdx.x == 0) st->pw = red.result[0];
+}
+
+// tea_leaf_cg_solve_calc_ur, tea_leaf_cg_cl.cl:73-137.  In the
+// device-resident loop alpha = rro/pw is formed here, and the block that
+// finishes the reduction carries out the host steps of one CG iteration
+// (tea_solve.f90:282-330): beta = rrn/rro, rro = rrn, error = sqrt(rrn) and
+// the exit test against eps * initial_residual.
+template <int TH>
+__global__ void __launch_bounds__(kBlock)
+    k_cg_calc_ur(Dev d, Red red, double alpha, ResState* st) {
+  if (st) {
+    if (*(volatile int*)&st->stop) return;
+    alpha = st->rro / st->pw;
+  }
+  const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (d.prec == PREC_JAC_BLOCK) {
+#pragma unroll 1
+      for (int ys = y0; ys < y0 + TH; ys += 4) {
+        double zl[4] = {0.0, 0.0, 0.0, 0.0}, rl[4] = {0.0, 0.0, 0.0, 0.0};
+        const long long c0 = cidx(d, x, ys);
+        if (xin && ys < d.y_max) {
+#pragma unroll
+          for (int i = 0; i < 4; i++) {
+            if (ys + i < d.y_max) {
+              const long long c = c0 + i * d.S;
+              d.u[c] = d.u[c] + alpha * d.p[c];
+              const double rv = d.r[c] - alpha * d.w[c];
+              d.r[c] = rv;
+              rl[i] = rv;
+            }
+          }
+          strip_solve(d, c0, strip_rows(d, ys), rl, zl);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          double v = 0.0;
+          if (xin && ys + i < d.y_max) {
+            d.z[c0 + i * d.S] = zl[i];
+            v = rl[i] * zl[i];
+          }
+          acc[0] = acc[0] + v;
+        }
+      }
+    } else {
+#pragma unroll 4
+      for (int j = 0; j < TH; j++) {
+        const int y = y0 + j;
+        double v = 0.0;
+        if (xin && y < d.y_max) {
+          const long long c = cidx(d, x, y);
+          d.u[c] = d.u[c] + alpha * d.p[c];
+          const double rv = d.r[c] - alpha * d.w[c];
+          d.r[c] = rv;
+          if (d.prec == PREC_JAC_DIAG) {
+            const double zv = rv * d.Mi[c];
+            d.z[c] = zv;
+            v = rv * zv;
+          } else {
+            v = rv * rv;
+          }
+        }
+        acc[0] = acc[0] + v;
+      }
+    }
+  });
+  if (st && last && threadIdx.x == 0) {
+    const double rrn = red.result[0];
+    const int n = st->n;
+    const double beta = rrn / st->rro;
+    st->alphas[n] = alpha;
+    st->betas[n] = beta;
+    st->alpha = alpha;
+    st->beta = beta;
+    st->rrn = rrn;
+    st->rro = rrn;
+    const double err = sqrt(rrn);
+    st->error = err;
+    st->p_pending = 1;
+    if (fabs(err) < st->eps_target) {
+      st->converged = 1;
+      st->stop = 1;
+    } else if (n >= st->loop_max) {
+      st->stop = 1;
+    } else {
+      st->n = n + 1;
+    }
+    __threadfence();
+  }
+}
+
+// tea_leaf_cg_solve_calc_p, tea_leaf_cg_cl.cl:141-160.  In the
+// device-resident loop it runs once per calc_ur that ran, with that
+// iteration's beta.
+template <int TH>
+__global__ void __launch_bounds__(kBlock)
+    k_cg_calc_p(Dev d, Red red, double beta, ResState* st,
+                unsigned int* counter) {
+  if (st) {
+    if (!*(volatile int*)&st->p_pending) return;
+    beta = st->beta;
+  }
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      if (y < d.y_max) {
+        const long long c = cidx(d, x, y);
+        if (d.prec != PREC_NONE)
+          d.p[c] = d.z[c] + beta * d.p[c];
+        else
+          d.p[c] = d.r[c] + beta * d.p[c];
+      }
+    }
+  });
+  if (st && last_block(counter) && threadIdx.x == 0) {
+    st->p_pending = 0;
+    __threadfence();
+  }
+}
+
+// The Chebyshev residual step shared by tea_leaf_cheby_solve_init_p and
+// tea_leaf_cheby_solve_calc_p (tea_leaf_cheby_cl.cl:4-64, :78-145):
+// w = A u, r = u0 - w, then p from M^-1 r.  mode 0: p = M^-1 r / theta;
+// mode 1: p = alpha p + beta M^-1 r.
+template <int TH>
+__global__ void __launch_bounds__(kBlock)
+    k_cheby_p(Dev d, Red red, int mode, double theta, double alpha,
+              double beta) {
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+    if (d.prec == PREC_JAC_BLOCK) {
+#pragma unroll 1
+      for (int ys = y0; ys < y0 + TH && ys < d.y_max; ys += 4) {
+        double zl[4], rl[4] = {0.0, 0.0, 0.0, 0.0};
+        const long long c0 = cidx(d, x, ys);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          if (ys + i < d.y_max) {
+            const long long c = c0 + i * d.S;
+            const double wv = smvp(d, d.u, c);
+            d.w[c] = wv;
+            const double rv = d.u0[c] - wv;
+            d.r[c] = rv;
+            rl[i] = rv;
+          }
+        }
+        strip_solve(d, c0, strip_rows(d, ys), rl, zl);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          if (ys + i < d.y_max) {
+            const long long c = c0 + i * d.S;
+            if (mode == 0)
+              d.p[c] = zl[i] / theta;
+            else
+              d.p[c] = alpha * d.p[c] + beta * zl[i];
+          }
+        }
+      }
+    } else {
+#pragma unroll 4
+      for (int j = 0; j < TH; j++) {
+        const int y = y0 + j;
+        if (y < d.y_max) {
+          const long long c = cidx(d, x, y);
+          const double wv = smvp(d, d.u, c);
+          d.w[c] = wv;
+          const double rv = d.u0[c] - wv;
+          d.r[c] = rv;
+          if (mode == 0) {
+            if (d.prec == PREC_JAC_DIAG)
+              d.p[c] = (d.Mi[c] * rv) / theta;
+            else
+              d.p[c] = rv / theta;
+          } else {
+            if (d.prec == PREC_JAC_DIAG)
+              d.p[c] = alpha * d.p[c] + beta * d.Mi[c] * rv;
+            else
+              d.p[c] = alpha * d.p[c] + beta * rv;
+          }
+        }
+      }
+    }
+  });
+}
+
+// tea_leaf_cheby_solve_calc_u, tea_leaf_cheby_cl.cl:66-76
+template <int TH>
+__global__ void __launch_bounds__(kBlock) k_cheby_calc_u(Dev d, Red red) {
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      if (y < d.y_max) {
+        const long long c = cidx(d, x, y);
+        d.u[c] = d.u[c] + d.p[c];
+      }
+    }
+  });
+}
+
+// M^-1 r with the PPCG forms: tea_leaf_ppcg_solve_init_sd
+// (tea_leaf_ppcg_cl.cl:4-60, mode 0: sd = M^-1 r / theta) and
+// tea_leaf_ppcg_solve_calc_sd (:90-155, mode 1: sd = alpha sd + beta M^-1 r)
+template <int TH>
+__global__ void __launch_bounds__(kBlock)
+    k_ppcg_sd(Dev d, Red red, int mode, double theta, double alpha,
+              double beta) {
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+    if (d.prec == PREC_JAC_BLOCK) {
+#pragma unroll 1
+      for (int ys = y0; ys < y0 + TH && ys < d.y_max; ys += 4) {
+        double zl[4], rl[4];
+        const long long c0 = cidx(d, x, ys);
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+          rl[i] = (ys + i < d.y_max) ? d.r[c0 + i * d.S] : 0.0;
+        strip_solve(d, c0, strip_rows(d, ys), rl, zl);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          if (ys + i < d.y_max) {
+            const long long c = c0 + i * d.S;
+            if (mode == 0)
+              d.sd[c] = zl[i] / theta;
+            else
+              d.sd[c] = alpha * d.sd[c] + beta * zl[i];
+          }
+        }
+      }
+    } else {
+#pragma unroll 4
+      for (int j = 0; j < TH; j++) {
+        const int y = y0 + j;
+        if (y < d.y_max) {
+          const long long c = cidx(d, x, y);
+          const double rv = d.r[c];
+          if (mode == 0) {
+            if (d.prec == PREC_JAC_DIAG)
+              d.sd[c] = rv * d.Mi[c] / theta;
+            else
+              d.sd[c] = rv / theta;
+          } else {
+            if (d.prec == PREC_JAC_DIAG)
+              d.sd[c] = alpha * d.sd[c] + beta * rv * d.Mi[c];
+            else
+              d.sd[c] = alpha * d.sd[c] + beta * rv;
+          }
+        }
+      }
+    }
+  });
+}
+
+// tea_leaf_ppcg_solve_update_r, tea_leaf_ppcg_cl.cl:62-88
+template <int TH>
+__global__ void __launch_bounds__(kBlock) k_ppcg_update_r(Dev d, Red red) {
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      if (y < d.y_max) {
+        const long long c = cidx(d, x, y);
+        d.u[c] = d.u[c] + d.sd[c];
+        const double result = smvp(d, d.sd, c);
+        d.r[c] = d.r[c] - result;
+      }
+    }
+  });
+}
+
+// tea_leaf_jacobi_copy_u, tea_leaf_jacobi_cl.cl:3-13 (un is vector_Mi, as
+// in the reference, ocl_kernels.cpp:576-585)
+template <int TH>
+__global__ void __launch_bounds__(kBlock) k_jacobi_copy_u(Dev d, Red red) {
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      if (y < d.y_max) {
+        const long long c = cidx(d, x, y);
+        d.un[c] = d.u[c];
+      }
+    }
+  });
+}
+
+// tea_leaf_jacobi_solve, tea_leaf_jacobi_cl.cl:15-42
+template <int TH>
+__global__ void __launch_bounds__(kBlock) k_jacobi_solve(Dev d, Red red) {
+  tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    const long long S = d.S;
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      double v = 0.0;
+      if (xin && y < d.y_max) {
+        const long long c = cidx(d, x, y);
+        const double* un = d.un;
+        const double kxc = d.Kx[c], kxe = d.Kx[c + 1];
+        const double kyc = d.Ky[c], kyn = d.Ky[c + S];
+        const double u1 = (d.u0[c] + kxe * un[c + 1] + kxc * un[c - 1] +
+                           kyn * un[c + S] + kyc * un[c - S]) /
+                          (1.0 + (kxc + kxe) + (kyc + kyn));
+        d.u[c] = u1;
+        v = fabs(u1 - un[c]);
+      }
+      acc[0] = acc[0] + v;
+    }
+  });
+}
+
+// tea_leaf_finalise, tea_leaf_common_cl.cl:4-15
+template <int TH>
+__global__ void __launch_bounds__(kBlock) k_finalise(Dev d, Red red) {
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      if (y < d.y_max) {
+        const long long c = cidx(d, x, y);
+        d.energy1[c] = d.u[c] / d.density[c];
+      }
+    }
+  });
+}
+
+// field_summary, field_summary_cl.cl:3-43 (energy argument bound to energy1,
+// ocl_kernels.cpp:466-469)
+template <int TH>
+__global__ void __launch_bounds__(kBlock) k_field_summary(Dev d, Red red) {
+  tile_driver<TH, 4>(d, red, [&](int x, int y0, bool xin, double* acc) {
+#pragma unroll 2
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+      if (xin && y < d.y_max) {
+        const long long c = cidx(d, x, y);
+        const double cell_vol = d.volume[c];
+        const double cell_mass = cell_vol * d.density[c];
+        v0 = cell_vol;
+        v1 = cell_mass;
+        v2 = cell_mass * d.energy1[c];
+        v3 = cell_mass * d.u[c];
+      }
+      acc[0] = acc[0] + v0;
+      acc[1] = acc[1] + v1;
+      acc[2] = acc[2] + v2;
+      acc[3] = acc[3] + v3;
+    }
+  });
+}
+
+// ---------------------------------------------------------------------------
+// launch wrappers
+// ---------------------------------------------------------------------------
+
+void launch_initialise_chunk(Chunk& c, double xmin, double ymin, double dx,
+                             double dy) {
+  const Dev d = c.dev();
+  const int n = std::max(d.x_max, d.y_max) + d.H + 1;
+  profile_begin("initialise_chunk_first");
+  k_init_chunk_1d<<<(n + 255) / 256, 256, 0, c.stream>>>(d, xmin, ymin, dx, dy);
+  count_launch("initialise_chunk_first");
+  check_cuda(cudaGetLastError(), "initialise_chunk_first");
+  profile_end("initialise_chunk_first");
+  launch_2d(c, "initialise_chunk_second", d.x_max + 2, d.y_max + 2, k_volume, d,
+            dx * dy);
+}
+
+void launch_generate_init(Chunk& c, double dens0, double en0) {
+  const Dev d = c.dev();
+  launch_2d(c, "generate_chunk_init", d.x_max, d.y_max, k_gen_init, d, dens0, en0);
+}
+
+void launch_generate_state(Chunk& c, double dens, double en, double xmin,
+                           double xmax, double ymin, double ymax,
+                           double radius, int geom, int g_rect, int g_circ,
+                           int g_point) {
+  const Dev d = c.dev();
+  launch_2d(c, "generate_chunk", d.x_max, d.y_max, k_gen_state, d, dens, en,
+            xmin, xmax, ymin, ymax, radius, geom, g_rect, g_circ, g_point);
+}
+
+void launch_init_u(Chunk& c, const double* energy) {
+  const Dev d = c.dev();
+  launch_2d(c, "generate_chunk_init_u", d.x_max, d.y_max, k_init_u, d, energy);
+}
+
+void launch_set_field(Chunk& c) {
+  const Dev d = c.dev();
+  launch_2d(c, "set_field", d.x_max, d.y_max, k_set_field, d);
+}
+
+void launch_init_common(Chunk& c, int coef, double rx, double ry) {
+  const Dev d = c.dev();
+  launch_2d(c, "tea_leaf_init_common", d.xs - 1, d.ys - 1, k_init_common, d,
+            coef, rx, ry);
+}
+
+void launch_zero_boundary(Chunk& c, const int* zb) {
+  const Dev d = c.dev();
+  launch_2d(c, "tea_leaf_zero_boundary", d.xs, d.ys, k_zero_boundary, d, zb[0],
+            zb[1], zb[2], zb[3]);
+}
+
+void launch_calc_residual(Chunk& c) {
+  TH_DISPATCH(c, "tea_leaf_calc_residual", k_calc_residual, c.dev(), c.red());
+}
+
+void launch_dot(Chunk& c, const double* a, const double* b) {
+  TH_DISPATCH(c, "tea_leaf_calc_2norm", k_dot, c.dev(), c.red(), a, b);
+}
+
+void launch_init_jac_diag(Chunk& c) {
+  const Dev d = c.dev();
+  launch_2d(c, "tea_leaf_init_jac_diag", d.xs, d.ys, k_init_jac_diag, d);
+}
+
+void launch_block_init(Chunk& c) {
+  const Dev d = c.dev();
+  launch_2d(c, "tea_leaf_block_init", d.x_max, (d.y_max + 3) / 4, k_block_init, d);
+}
+
+void launch_cg_init_p(Chunk& c) {
+  TH_DISPATCH(c, "tea_leaf_cg_solve_init_p", k_cg_init_p, c.dev(), c.red());
+}
+
+void launch_cg_calc_w(Chunk& c) {
+  TH_DISPATCH(c, "tea_leaf_cg_solve_calc_w", k_cg_calc_w, c.dev(), c.red(),
+              (ResState*)nullptr);
+}
+
+void launch_cg_calc_ur(Chunk& c, double alpha) {
+  TH_DISPATCH(c, "tea_leaf_cg_solve_calc_ur", k_cg_calc_ur, c.dev(), c.red(),
+              alpha, (ResState*)nullptr);
+}
+
+void launch_cg_calc_p(Chunk& c, double beta) {
+  TH_DISPATCH(c, "tea_leaf_cg_solve_calc_p", k_cg_calc_p, c.dev(), c.red(), beta,
+              (ResState*)nullptr, (unsigned int*)nullptr);
+}
+
+void launch_cheby_init_p(Chunk& c, double theta) {
+  TH_DISPATCH(c, "tea_leaf_cheby_solve_init_p", k_cheby_p, c.dev(), c.red(), 0,
+              theta, 0.0, 0.0);
+}
+
+void launch_cheby_calc_p(Chunk& c, double alpha, double beta) {
+  TH_DISPATCH(c, "tea_leaf_cheby_solve_calc_p", k_cheby_p, c.dev(), c.red(), 1,
+              0.0, alpha, beta);
+}
+
+void launch_cheby_calc_u(Chunk& c) {
+  TH_DISPATCH(c, "tea_leaf_cheby_solve_calc_u", k_cheby_calc_u, c.dev(), c.red());
+}
+
+void launch_ppcg_init_sd(Chunk& c, double theta) {
+  TH_DISPATCH(c, "tea_leaf_ppcg_solve_init_sd", k_ppcg_sd, c.dev(), c.red(), 0,
+              theta, 0.0, 0.0);
+}
+
+void launch_ppcg_update_r(Chunk& c) {
+  TH_DISPATCH(c, "tea_leaf_ppcg_solve_update_r", k_ppcg_update_r, c.dev(),
+              c.red());
+}
+
+void launch_ppcg_calc_sd(Chunk& c, double alpha, double beta) {
+  TH_DISPATCH(c, "tea_leaf_ppcg_solve_calc_sd", k_ppcg_sd, c.dev(), c.red(), 1,
+              0.0, alpha, beta);
+}
+
+void launch_jacobi_copy_u(Chunk& c) {
+  TH_DISPATCH(c, "tea_leaf_jacobi_copy_u", k_jacobi_copy_u, c.dev(), c.red());
+}
+
+void launch_jacobi_solve(Chunk& c) {
+  TH_DISPATCH(c, "tea_leaf_jacobi_solve", k_jacobi_solve, c.dev(), c.red());
+}
+
+void launch_finalise(Chunk& c) {
+  TH_DISPATCH(c, "tea_leaf_finalise", k_finalise, c.dev(), c.red());
+}
+
+void launch_field_summary(Chunk& c) {
+  TH_DISPATCH(c, "field_summary", k_field_summary, c.dev(), c.red());
+}
+
+void launch_update_halo(Chunk& c, int mask, int depth) {
+  const Dev d = c.dev();
+  if (!mask || depth < 1) return;
+  launch_2d(c, "update_halo", d.x_max + 2 * depth, d.y_max + 2 * depth,
+            k_update_halo, d, mask, depth);
+}
+
+// ---------------------------------------------------------------------------
+// device-resident CG loop
+// ---------------------------------------------------------------------------
+
+// Grid size of a tile kernel: every SM filled once, capped by the number of
+// supertiles.
+template <class... KArgs>
+static int tile_grid(Chunk& c, void (*kernel)(KArgs...)) {
+  const long long cap = (long long)c.num_sms * blocks_per_sm((const void*)kernel);
+  return (int)std::max<long long>(1, std::min<long long>(c.dev().ns, cap));
+}
+
+template <int TH>
+static void enqueue_resident_iterations(Chunk& c, int iters) {
+  const Dev d = c.dev();
+  const Red red = c.red();
+  const int gw = tile_grid(c, k_cg_calc_w<TH>);
+  const int gu = tile_grid(c, k_cg_calc_ur<TH>);
+  const int gp = tile_grid(c, k_cg_calc_p<TH>);
+  for (int i = 0; i < iters; i++) {
+    k_cg_calc_w<TH><<<gw, kBlock, 0, c.stream>>>(d, red, c.res_state);
+    k_cg_calc_ur<TH><<<gu, kBlock, 0, c.stream>>>(d, red, 0.0, c.res_state);
+    k_cg_calc_p<TH><<<gp, kBlock, 0, c.stream>>>(d, red, 0.0, c.res_state,
+                                                 c.res_counter);
+  }
+}
+
+void resident_release() {
+  Chunk& c = chunk();
+  if (c.res_graph) cudaGraphExecDestroy(c.res_graph);
+  c.res_graph = nullptr;
+  c.res_graph_iters = 0;
+  cudaFree(c.res_state);
+  cudaFree(c.res_coef);
+  cudaFree(c.res_counter);
+  cudaFreeHost(c.res_state_h);
+  c.res_state = nullptr;
+  c.res_coef = nullptr;
+  c.res_counter = nullptr;
+  c.res_state_h = nullptr;
+  c.res_coef_n = 0;
+}
+
+// CG iterations n_begin..loop_max of tea_solve.f90:147-332 with all scalars
+// on the device.  The iterations are queued in batches replayed from a
+// captured CUDA graph; after each batch the host reads the loop state once.
+// Kernels queued after the loop has stopped return at once.  The arithmetic
+// and the exit test are those of the per-call path, so the results are
+// bit-identical to it.
+int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
+                           double eps_target, double* rro_out,
+                           double* error_out, int* n_done, int* converged,
+                           double* cg_alphas, double* cg_betas) {
+  Chunk& c = chunk();
+  const int batch = 16;
+  if (c.res_coef_n < loop_max + 2) {
+    cudaFree(c.res_coef);
+    c.res_coef = nullptr;
+    if (!check_cuda(cudaMalloc(&c.res_coef, 2 * sizeof(double) * (loop_max + 2)),
+                    "cudaMalloc resident coefficients"))
+      return -1;
+    c.res_coef_n = loop_max + 2;
+  }
+  if (!c.res_state) {
+    if (!check_cuda(cudaMalloc(&c.res_state, sizeof(ResState)), "cudaMalloc state") ||
+        !check_cuda(cudaMallocHost(&c.res_state_h, sizeof(ResState)),
+                    "cudaMallocHost state") ||
+        !check_cuda(cudaMalloc(&c.res_counter, sizeof(unsigned int)),
+                    "cudaMalloc counter"))
+      return -1;
+    cudaMemsetAsync(c.res_counter, 0, sizeof(unsigned int), c.stream);
+  }
+  ResState& h = *c.res_state_h;
+  memset(&h, 0, sizeof(h));
+  h.rro = rro_in;
+  h.eps_target = eps_target;
+  h.n = n_begin;
+  h.loop_max = loop_max;
+  h.alphas = c.res_coef;
+  h.betas = c.res_coef + c.res_coef_n;
+  if (!check_cuda(cudaMemcpyAsync(c.res_state, &h, sizeof(ResState),
+                                  cudaMemcpyHostToDevice, c.stream),
+                  "resident state upload"))
+    return -1;
+  if (!c.res_graph && !c.profiler_on) {
+    cudaGraph_t graph = nullptr;
+    if (!check_cuda(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal),
+                    "graph capture"))
+      return -1;
+    if (c.TH == 16)
+      enqueue_resident_iterations<16>(c, batch);
+    else
+      enqueue_resident_iterations<4>(c, batch);
+    if (!check_cuda(cudaStreamEndCapture(c.stream, &graph), "graph capture end") ||
+        !check_cuda(cudaGraphInstantiate(&c.res_graph, graph, 0), "graph instantiate"))
+      return -1;
+    cudaGraphDestroy(graph);
+    c.res_graph_iters = batch;
+  }
+  // every batch runs at least one iteration until the loop stops, so the
+  // loop needs at most this many batches; more means the state is corrupt
+  const long long max_batches = (long long)(loop_max - n_begin) / batch + 3;
+  for (long long nb = 0;; nb++) {
+    if (nb >= max_batches) {
+      fail(24, "resident CG loop did not stop after %lld batches", nb);
+      return -1;
+    }
+    if (c.res_graph) {
+      if (!check_cuda(cudaGraphLaunch(c.res_graph, c.stream), "graph launch"))
+        return -1;
+    } else {
+      if (c.TH == 16)
+        enqueue_resident_iterations<16>(c, batch);
+      else
+        enqueue_resident_iterations<4>(c, batch);
+      check_cuda(cudaGetLastError(), "resident launch");
+    }
+    for (int i = 0; i < 3 * batch; i++) count_launch("resident_cg");
+    if (!check_cuda(cudaMemcpyAsync(&h, c.res_state, sizeof(ResState),
+                                    cudaMemcpyDeviceToHost, c.stream),
+                    "resident state read") ||
+        !check_cuda(cudaStreamSynchronize(c.stream), "resident sync"))
+      return -1;
+    if (h.stop && !h.p_pending) break;
+  }
+  *rro_out = h.rro;
+  *error_out = h.error;
+  *n_done = h.n;
+  *converged = h.converged;
+  if (cg_alphas && cg_betas) {
+    const int n = h.n - n_begin + 1;
+    cudaMemcpyAsync(cg_alphas + n_begin, c.res_coef + n_begin, n * sizeof(double),
+                    cudaMemcpyDeviceToHost, c.stream);
+    cudaMemcpyAsync(cg_betas + n_begin, c.res_coef + c.res_coef_n + n_begin,
+                    n * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+    if (!check_cuda(cudaStreamSynchronize(c.stream), "resident coefficients"))
+      return -1;
+  }
+  return 0;
+}
+
+}  // namespace tea

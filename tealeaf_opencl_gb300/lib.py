@@ -1,0 +1,338 @@
+"""ctypes binding of libtealeaf_gb300.so (the C ABI in include/tealeaf_gb300.h).
+
+The library is the product: every call here goes to hand-written CUDA
+kernels for sm_103a.  There is no CPU fallback; if the shared library is
+missing and cannot be built, load() raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+FIELD = dict(density=1, energy0=2, energy1=3, u=4, p=5, sd=6, r=7, u0=8, w=9,
+             z=10, Mi=11, Kx=12, Ky=13, cp=14, bfp=15, volume=16)
+PREC = dict(none=1, jac_diag=2, jac_block=3)
+SOLVER = dict(jacobi=1, cg=2, chebyshev=3, ppcg=4)
+EXTERNAL_FACE = -1
+DRIVER_PER_CALL = 0
+DRIVER_RESIDENT = 1
+
+# the C-ABI entry points declared in include/tealeaf_gb300.h
+REFERENCE_SYMBOLS = [
+    "initialise_ocl_", "initialise_chunk_kernel_ocl_", "generate_chunk_kernel_ocl_",
+    "set_field_kernel_ocl_", "field_summary_kernel_ocl_", "update_halo_kernel_ocl_",
+    "tea_leaf_common_init_kernel_ocl_", "tea_leaf_calc_residual_ocl_",
+    "tea_leaf_calc_2norm_kernel_ocl_", "tea_leaf_cg_init_kernel_ocl_",
+    "tea_leaf_cg_calc_w_kernel_ocl_", "tea_leaf_cg_calc_ur_kernel_ocl_",
+    "tea_leaf_cg_calc_p_kernel_ocl_", "tea_leaf_cheby_init_kernel_ocl_",
+    "tea_leaf_cheby_iterate_kernel_ocl_", "tea_leaf_ppcg_init_ocl_",
+    "tea_leaf_ppcg_init_sd_kernel_ocl_", "tea_leaf_ppcg_inner_kernel_ocl_",
+    "tea_leaf_jacobi_solve_kernel_ocl_", "tea_leaf_common_finalise_kernel_ocl_",
+    "print_opencl_profiling_info_", "ocl_pack_buffers_", "ocl_unpack_buffers_",
+]
+EXTRA_SYMBOLS = [
+    "tea_gb300_configure", "tea_gb300_set_abort_on_error", "tea_gb300_last_error",
+    "tea_gb300_finalise", "tea_gb300_read_field", "tea_gb300_write_field",
+    "tea_gb300_read_field_padded", "tea_gb300_write_field_padded",
+    "tea_gb300_reduction_rows", "tea_gb300_kernel_launches", "tea_gb300_stream",
+    "tea_gb300_chunk_info", "tea_gb300_event_record", "tea_gb300_event_elapsed_ms",
+    "tea_gb300_synchronize", "tea_gb300_host_alloc", "tea_gb300_host_free",
+    "tea_gb300_kernel_timer_select", "tea_gb300_kernel_timer_read",
+    "tea_gb300_driver_open", "tea_gb300_driver_step", "tea_gb300_driver_close",
+]
+
+
+class StepInfo(C.Structure):
+    _fields_ = [
+        ("step", C.c_int), ("time", C.c_double), ("dt", C.c_double),
+        ("iterations", C.c_int), ("inner_iterations", C.c_int),
+        ("conduction_error", C.c_double), ("exact_error", C.c_double),
+        ("summary_done", C.c_int), ("vol", C.c_double), ("mass", C.c_double),
+        ("ie", C.c_double), ("temp", C.c_double), ("complete", C.c_int),
+        ("qa_passed", C.c_int), ("qa_diff", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class TeaError(RuntimeError):
+    pass
+
+
+_lib = None
+PI = C.POINTER(C.c_int)
+PD = C.POINTER(C.c_double)
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build=True):
+    """Load the CUDA library (building it with nvcc first if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build else _build.LIB
+    if not os.path.exists(path):
+        raise TeaError("libtealeaf_gb300.so not found at %s" % path)
+    L = C.CDLL(path)
+    d, i, v = C.c_double, C.c_int, None
+    sig = {
+        "initialise_ocl_": (v, [PI, PI, PI, PI]),
+        "initialise_chunk_kernel_ocl_": (v, [PD, PD, PD, PD]),
+        "generate_chunk_kernel_ocl_": (v, [PI, PD, PD, PD, PD, PD, PD, PD, PI, PI, PI, PI]),
+        "set_field_kernel_ocl_": (v, []),
+        "field_summary_kernel_ocl_": (v, [PD, PD, PD, PD]),
+        "update_halo_kernel_ocl_": (v, [PI, PI, PI]),
+        "tea_leaf_common_init_kernel_ocl_": (v, [PI, PD, PD, PD, PI, PI]),
+        "tea_leaf_calc_residual_ocl_": (v, []),
+        "tea_leaf_calc_2norm_kernel_ocl_": (v, [PI, PD]),
+        "tea_leaf_cg_init_kernel_ocl_": (v, [PD]),
+        "tea_leaf_cg_calc_w_kernel_ocl_": (v, [PD]),
+        "tea_leaf_cg_calc_ur_kernel_ocl_": (v, [PD, PD]),
+        "tea_leaf_cg_calc_p_kernel_ocl_": (v, [PD]),
+        "tea_leaf_cheby_init_kernel_ocl_": (v, [PD, PD, PI, PD, PD, PD]),
+        "tea_leaf_cheby_iterate_kernel_ocl_": (v, [PI]),
+        "tea_leaf_ppcg_init_ocl_": (v, [PD, PD, PD, PI]),
+        "tea_leaf_ppcg_init_sd_kernel_ocl_": (v, []),
+        "tea_leaf_ppcg_inner_kernel_ocl_": (v, [PI, PI, PI]),
+        "tea_leaf_jacobi_solve_kernel_ocl_": (v, [PD]),
+        "tea_leaf_common_finalise_kernel_ocl_": (v, []),
+        "print_opencl_profiling_info_": (v, []),
+        "ocl_pack_buffers_": (v, [PI, PI, PI, PI, PD]),
+        "ocl_unpack_buffers_": (v, [PI, PI, PI, PI, PD]),
+        "tea_gb300_configure": (i, [i, i, i, i]),
+        "tea_gb300_set_abort_on_error": (v, [i]),
+        "tea_gb300_last_error": (i, [C.c_char_p, i]),
+        "tea_gb300_finalise": (v, []),
+        "tea_gb300_read_field": (i, [i, PD]),
+        "tea_gb300_write_field": (i, [i, PD]),
+        "tea_gb300_read_field_padded": (i, [i, PD]),
+        "tea_gb300_write_field_padded": (i, [i, PD]),
+        "tea_gb300_reduction_rows": (i, [i, i]),
+        "tea_gb300_kernel_launches": (C.c_longlong, []),
+        "tea_gb300_stream": (C.c_void_p, []),
+        "tea_gb300_chunk_info": (i, [PI, PI, PI, PI]),
+        "tea_gb300_event_record": (i, [i]),
+        "tea_gb300_event_elapsed_ms": (C.c_float, [i, i]),
+        "tea_gb300_synchronize": (i, []),
+        "tea_gb300_host_alloc": (C.c_void_p, [C.c_size_t]),
+        "tea_gb300_host_free": (v, [C.c_void_p]),
+        "tea_gb300_kernel_timer_select": (i, [C.c_char_p]),
+        "tea_gb300_kernel_timer_read": (i, [PD, C.POINTER(C.c_longlong)]),
+        "tea_gb300_driver_open": (i, [C.c_char_p, C.c_char_p, i, i]),
+        "tea_gb300_driver_step": (i, [C.POINTER(StepInfo)]),
+        "tea_gb300_driver_close": (v, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    L.tea_gb300_set_abort_on_error(0)
+    _lib = L
+    return L
+
+
+def check():
+    """Raise TeaError if the library recorded an error since the last check."""
+    buf = C.create_string_buffer(1024)
+    code = load().tea_gb300_last_error(buf, 1024)
+    if code:
+        raise TeaError("libtealeaf_gb300 error %d: %s" % (code, buf.value.decode()))
+
+
+def _ip(v):
+    return C.byref(C.c_int(int(v)))
+
+
+def _dp(v):
+    return C.byref(C.c_double(float(v)))
+
+
+def _pd(a):
+    return a.ctypes.data_as(PD)
+
+
+def _pi(a):
+    return a.ctypes.data_as(PI)
+
+
+class Chunk:
+    """The process-global chunk, driven through the reference's entry points."""
+
+    def __init__(self, x_max, y_max, halo=1, solver="cg", prec="none"):
+        L = load()
+        s = SOLVER[solver] if isinstance(solver, str) else int(solver)
+        p = PREC[prec] if isinstance(prec, str) else int(prec)
+        if L.tea_gb300_configure(int(halo), s, p, 0) != 0:
+            raise TeaError("invalid configuration")
+        L.initialise_ocl_(_ip(1), _ip(x_max), _ip(1), _ip(y_max))
+        check()
+        self.x_max, self.y_max, self.halo = x_max, y_max, halo
+        self.neighbours = np.full(4, EXTERNAL_FACE, dtype=np.int32)
+
+    # -- setup -------------------------------------------------------------
+    def initialise_chunk(self, xmin, ymin, dx, dy):
+        load().initialise_chunk_kernel_ocl_(_dp(xmin), _dp(ymin), _dp(dx), _dp(dy))
+        check()
+
+    def generate_chunk(self, density, energy, xmin, xmax, ymin, ymax, radius, geometry):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64)
+                for a in (density, energy, xmin, xmax, ymin, ymax, radius)]
+        geom = np.ascontiguousarray(geometry, dtype=np.int32)
+        load().generate_chunk_kernel_ocl_(_ip(len(geom)), *[_pd(a) for a in arrs],
+                                          _pi(geom), _ip(1), _ip(2), _ip(3))
+        check()
+
+    def set_field(self):
+        load().set_field_kernel_ocl_()
+        check()
+
+    # -- solver entry points -----------------------------------------------
+    def common_init(self, coefficient, dt, zero_boundary=(1, 1, 1, 1), reflective=0):
+        rx, ry = C.c_double(), C.c_double()
+        zb = np.ascontiguousarray(zero_boundary, dtype=np.int32)
+        load().tea_leaf_common_init_kernel_ocl_(_ip(coefficient), _dp(dt), C.byref(rx),
+                                                C.byref(ry), _pi(zb), _ip(reflective))
+        check()
+        return rx.value, ry.value
+
+    def calc_residual(self):
+        load().tea_leaf_calc_residual_ocl_()
+        check()
+
+    def _scalar(self, fn, *args):
+        out = C.c_double()
+        fn(*args, C.byref(out))
+        check()
+        return out.value
+
+    def calc_2norm(self, which):
+        return self._scalar(load().tea_leaf_calc_2norm_kernel_ocl_, _ip(which))
+
+    def cg_init(self):
+        return self._scalar(load().tea_leaf_cg_init_kernel_ocl_)
+
+    def cg_calc_w(self):
+        return self._scalar(load().tea_leaf_cg_calc_w_kernel_ocl_)
+
+    def cg_calc_ur(self, alpha):
+        return self._scalar(load().tea_leaf_cg_calc_ur_kernel_ocl_, _dp(alpha))
+
+    def cg_calc_p(self, beta):
+        load().tea_leaf_cg_calc_p_kernel_ocl_(_dp(beta))
+        check()
+
+    def cheby_init(self, alphas, betas, theta, rx=0.0, ry=0.0):
+        a = np.ascontiguousarray(alphas, dtype=np.float64)
+        b = np.ascontiguousarray(betas, dtype=np.float64)
+        load().tea_leaf_cheby_init_kernel_ocl_(_pd(a), _pd(b), _ip(len(a)), _dp(rx),
+                                               _dp(ry), _dp(theta))
+        check()
+
+    def cheby_iterate(self, step):
+        load().tea_leaf_cheby_iterate_kernel_ocl_(_ip(step))
+        check()
+
+    def ppcg_init(self, alphas, betas, theta):
+        a = np.ascontiguousarray(alphas, dtype=np.float64)
+        b = np.ascontiguousarray(betas, dtype=np.float64)
+        load().tea_leaf_ppcg_init_ocl_(_pd(a), _pd(b), _dp(theta), _ip(len(a)))
+        check()
+
+    def ppcg_init_sd(self):
+        load().tea_leaf_ppcg_init_sd_kernel_ocl_()
+        check()
+
+    def ppcg_inner(self, step, bounds_extra=0):
+        load().tea_leaf_ppcg_inner_kernel_ocl_(_ip(step), _ip(bounds_extra),
+                                               _pi(self.neighbours))
+        check()
+
+    def jacobi_solve(self):
+        return self._scalar(load().tea_leaf_jacobi_solve_kernel_ocl_)
+
+    def finalise(self):
+        load().tea_leaf_common_finalise_kernel_ocl_()
+        check()
+
+    def field_summary(self):
+        out = [C.c_double() for _ in range(4)]
+        load().field_summary_kernel_ocl_(*[C.byref(o) for o in out])
+        check()
+        return tuple(o.value for o in out)
+
+    def update_halo(self, fields, depth):
+        f = np.ascontiguousarray(fields, dtype=np.int32)
+        load().update_halo_kernel_ocl_(_pi(self.neighbours), _pi(f), _ip(depth))
+        check()
+
+    # -- field access -------------------------------------------------------
+    def read(self, name):
+        out = np.zeros((self.y_max, self.x_max))
+        if load().tea_gb300_read_field(FIELD[name], _pd(out)) != 0:
+            check()
+        return out
+
+    def write(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        assert a.shape == (self.y_max, self.x_max)
+        if load().tea_gb300_write_field(FIELD[name], _pd(a)) != 0:
+            check()
+
+    def read_padded(self, name):
+        out = np.zeros((self.y_max + 2 * self.halo, self.x_max + 2 * self.halo))
+        if load().tea_gb300_read_field_padded(FIELD[name], _pd(out)) != 0:
+            check()
+        return out
+
+    def write_padded(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        assert a.shape == (self.y_max + 2 * self.halo, self.x_max + 2 * self.halo)
+        if load().tea_gb300_write_field_padded(FIELD[name], _pd(a)) != 0:
+            check()
+
+
+class Driver:
+    """The whole-run driver: tea.in text in, one timestep per step()."""
+
+    def __init__(self, deck_text, mode=DRIVER_PER_CALL, max_iters_cap=0, log_path=None):
+        L = load()
+        rc = L.tea_gb300_driver_open(deck_text.encode(),
+                                     log_path.encode() if log_path else None,
+                                     int(mode), int(max_iters_cap))
+        if rc != 0:
+            check()
+            raise TeaError("driver_open failed")
+
+    def step(self):
+        info = StepInfo()
+        rc = load().tea_gb300_driver_step(C.byref(info))
+        if rc < 0:
+            check()
+            raise TeaError("driver_step failed")
+        return None if rc == 1 else info
+
+    def close(self):
+        load().tea_gb300_driver_close()
+
+
+def run_deck(deck_text, mode=DRIVER_PER_CALL, max_iters_cap=0, log_path=None):
+    """Run a deck to completion; returns the list of per-step StepInfo."""
+    drv = Driver(deck_text, mode, max_iters_cap, log_path)
+    steps = []
+    try:
+        while True:
+            info = drv.step()
+            if info is None:
+                break
+            steps.append(info)
+            if info.complete:
+                break
+    finally:
+        drv.close()
+    return steps

@@ -1,0 +1,44 @@
+"""Records the CPU oracle's results for the long CG test problems.
+
+tests/test_gpu_runs.py compares the GPU runs of test problems 2 and 3
+(960^2 and 3840^2 CG, tens of thousands of iterations) with these records
+bit for bit: per-step iteration counts and the final temperature (as a hex
+float).  The oracle takes minutes to hours on a CPU for these, so the
+results are kept as a fixture.  Usage: make_oracle_pins.py TP [TP ...]
+"""
+import json
+import os
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from oracle import oracle  # noqa: E402
+
+
+def main(tps):
+    path = os.path.join(HERE, "oracle_pins.json")
+    pins = json.load(open(path)) if os.path.exists(path) else {}
+    meta = json.load(open(os.path.join(HERE, "test_problems.json")))
+    for tp in tps:
+        p = meta["problems"][str(tp)]
+        deck = open(os.path.join(HERE, p["deck"])).read()
+        t0 = time.time()
+        res = oracle.run_deck(deck)
+        pins[str(tp)] = {
+            "deck": p["deck"],
+            "temp": res.final_temp,
+            "temp_hex": float(res.final_temp).hex(),
+            "golden_temp": p["temp"],
+            "qa_diff_percent": res.qa_diff,
+            "iterations": list(res.iterations[:res.n_steps]),
+            "oracle_threads": oracle.lib().oracle_num_threads(),
+            "oracle_seconds": round(time.time() - t0, 1),
+        }
+        json.dump(pins, open(path, "w"), indent=1, sort_keys=True)
+        print(tp, res.final_temp, res.qa_diff, flush=True)
+
+
+if __name__ == "__main__":
+    main([int(a) for a in sys.argv[1:]] or [2])

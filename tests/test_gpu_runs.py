@@ -1,0 +1,101 @@
+"""Whole tea.in decks on the GPU: reference goldens and oracle parity.
+
+The C++ driver restates the reference's Fortran driver on top of the C ABI.
+Each run must (a) pass the reference's own test-problem check
+(field_summary.f90:88-106, 0.001 %) where the deck is a test problem and
+(b) match the oracle's run of the same deck bit for bit: the same iteration
+count in every timestep and the same field_summary values.
+"""
+import json
+import os
+
+import pytest
+
+from oracle import oracle
+from tealeaf_opencl_gb300 import decks, lib
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def problem(tp):
+    meta = json.load(open(os.path.join(GOLD, "test_problems.json")))
+    p = meta["problems"][str(tp)]
+    return open(os.path.join(GOLD, p["deck"])).read(), p["temp"]
+
+
+def pins():
+    path = os.path.join(GOLD, "oracle_pins.json")
+    return json.load(open(path)) if os.path.exists(path) else {}
+
+
+def gpu_run(deck, mode=lib.DRIVER_PER_CALL):
+    steps = lib.run_deck(deck, mode=mode)
+    assert steps and steps[-1].complete
+    return steps
+
+
+def assert_matches_oracle(steps, res):
+    assert len(steps) == res.n_steps
+    assert [s.iterations for s in steps] == list(res.iterations[:res.n_steps])
+    assert [s.inner_iterations for s in steps] == list(res.inner_iterations[:res.n_steps])
+    last = steps[-1]
+    final = res.summaries()[-1]
+    assert (last.vol, last.mass, last.ie, last.temp) == tuple(final[[1, 2, 4, 5]])
+
+
+@pytest.mark.parametrize("tp", [1, 6])
+def test_test_problem_matches_golden_and_oracle(tp):
+    deck, temp = problem(tp)
+    steps = gpu_run(deck)
+    assert steps[-1].qa_passed == 1, steps[-1].qa_diff
+    assert abs(100.0 * steps[-1].temp / temp - 100.0) < 0.001
+    assert_matches_oracle(steps, oracle.run_deck(deck))
+
+
+@pytest.mark.parametrize("tp", [2, 3])
+def test_cg_test_problem_matches_golden_and_oracle_pin(tp):
+    deck, temp = problem(tp)
+    steps = gpu_run(deck, mode=lib.DRIVER_RESIDENT)
+    assert steps[-1].qa_passed == 1, steps[-1].qa_diff
+    pin = pins().get(str(tp))
+    if pin is None:
+        pytest.skip("no oracle pin recorded for test problem %d" % tp)
+    assert [s.iterations for s in steps] == pin["iterations"]
+    assert steps[-1].temp == float.fromhex(pin["temp_hex"])
+
+
+@pytest.mark.parametrize("tp", [4, 5])
+def test_long_cg_test_problems_match_golden(tp):
+    deck, temp = problem(tp)
+    steps = gpu_run(deck, mode=lib.DRIVER_RESIDENT)
+    assert steps[-1].qa_passed == 1, steps[-1].qa_diff
+
+
+def test_c1_512_cg_jac_diag_matches_oracle():
+    """512x512 CG + diagonal Jacobi, eps 1e-15, 10 steps."""
+    deck = decks.five_state_deck(512, solver="cg", prec="jac_diag", steps=10,
+                                 eps=1e-15, max_iters=5000)
+    res = oracle.run_deck(deck)
+    per_call = gpu_run(deck)
+    assert_matches_oracle(per_call, res)
+    resident = gpu_run(deck, mode=lib.DRIVER_RESIDENT)
+    assert_matches_oracle(resident, res)
+
+
+@pytest.mark.parametrize("solver,prec", [("chebyshev", "jac_block"), ("ppcg", "jac_block"),
+                                         ("chebyshev", "jac_diag"), ("ppcg", "none")])
+def test_cheby_ppcg_decks_match_oracle(solver, prec):
+    deck = decks.five_state_deck(256, solver=solver, prec=prec, steps=4, eps=1e-15,
+                                 max_iters=5000, halo=2, inner_steps=10, presteps=20)
+    assert_matches_oracle(gpu_run(deck), oracle.run_deck(deck))
+
+
+def test_reflective_check_result_deck_matches_oracle():
+    deck = decks.five_state_deck(123, solver="cg", prec="jac_block", steps=3, eps=1e-12,
+                                 y_cells=99, reflective=True, check_result=True,
+                                 coefficient="inverse")
+    steps = gpu_run(deck)
+    res = oracle.run_deck(deck)
+    assert_matches_oracle(steps, res)
+    assert [s.exact_error for s in steps] == list(res.exact_error[:res.n_steps])
