@@ -11,9 +11,10 @@ before the switch, tl_eps 1e-15, FP64.  W untimed steps run first (the
 first contains the CG steps and the eigenvalue estimate); K steps are timed
 with CUDA events on the library's stream.
 
-value : cell-iterations/s (interior cells x outer solver iterations / s)
-        with the fields resident in HBM, through the library's fastest
-        driver mode.
+value : cell-iterations/s (interior cells x solver iterations / s, counting
+        outer plus PPCG inner iterations as the reference's "Total" count
+        does) with the fields resident in HBM, through the library's
+        fastest driver mode.
 e2e   : the same metric through the per-call C ABI (two host round trips
         per CG iteration, as the reference's Fortran makes them), with each
         step's input fields (density, energy1) copied host->device from
@@ -51,16 +52,20 @@ WORKLOADS = {
 }
 
 
+ARITHMETIC = "fused"
+
+
 def deck_for(name, steps):
     from tealeaf_opencl_gb300 import decks
     cells, solver, prec, halo, inner, presteps, eps = WORKLOADS[name][:7]
-    # tl_ch_cg_epslim large: the switch to Chebyshev/PPCG happens right after
-    # the tl_ch_cg_presteps CG steps that estimate the eigenvalues
-    extra = "tl_ch_cg_epslim=1.0e300" if solver in ("ppcg", "chebyshev") else ""
+    # C1 names tl_max_iters 5000; the 4096^2 configuration names none, so
+    # the reference's default of 1000 (read_input.f90:59) applies
+    max_iters = 5000 if cells <= 512 else 1000
     return decks.five_state_deck(cells, solver=solver, prec=prec, steps=steps,
-                                 eps=eps, max_iters=5000, halo=halo,
+                                 eps=eps, max_iters=max_iters, halo=halo,
                                  inner_steps=inner, presteps=presteps,
-                                 summary_frequency=0, extra=extra)
+                                 summary_frequency=0,
+                                 extra="tl_arithmetic %s" % ARITHMETIC)
 
 
 def config_for(name):
@@ -72,7 +77,10 @@ def config_for(name):
            "domain": "[0,10]^2, five reference states",
            "l2": "inputs larger than L2: each FP64 field is %.0f MB, the "
                  "solve touches about 12 of them" % (cells * cells * 8 / 1e6),
-           "parallelism": "replicas"}
+           "arithmetic": ARITHMETIC,
+           "iteration_count": "outer + PPCG inner (the reference's 'Total')",
+           "parallelism": "replicas",
+           "tl_max_iters": 5000 if cells <= 512 else 1000}
     if solver == "ppcg":
         cfg["inner_steps"] = inner
     if solver in ("ppcg", "chebyshev"):
@@ -213,7 +221,7 @@ def run_ours(args, dist):
     deck = deck_for(name, steps_total)
 
     # ---- value: fields resident in HBM, fastest driver mode ----
-    drv = lib.Driver(deck, mode=lib.DRIVER_RESIDENT)
+    drv = lib.Driver(deck, mode=lib.DRIVER_RESIDENT, max_iters_cap=args.cap)
     for _ in range(args.warmup):
         drv.step()
     L.tea_gb300_kernel_timer_select(kernel.encode())
@@ -239,11 +247,11 @@ def run_ours(args, dist):
     outer = sum(i.iterations for i in infos)
     inner = sum(i.inner_iterations for i in infos)
     ms_max = dist.max(ms)
-    outer_all = dist.sum(outer)
-    value = outer_all * ncell / (ms_max / 1e3)
+    total_all = dist.sum(outer + inner)
+    value = total_all * ncell / (ms_max / 1e3)
 
     # ---- e2e: per-call C ABI, host buffers, copies inside the timed region ----
-    drv = lib.Driver(deck, mode=lib.DRIVER_PER_CALL)
+    drv = lib.Driver(deck, mode=lib.DRIVER_PER_CALL, max_iters_cap=args.cap)
     for _ in range(args.warmup):
         drv.step()
     nbytes = ncell * 8
@@ -264,7 +272,7 @@ def run_ours(args, dist):
         info = drv.step()
         chunk_read("energy1", host[2])
         host[1][...] = host[2]
-        e2e_outer += info.iterations
+        e2e_outer += info.iterations + info.inner_iterations
     L.tea_gb300_synchronize()
     e2e_s = time.perf_counter() - t0
     dist.barrier()
@@ -294,7 +302,7 @@ def run_ours(args, dist):
         "config": config_for(name),
         "iterations": {"outer": outer, "ppcg_inner": inner,
                        "per_step": [i.iterations for i in infos]},
-        "total_cell_iters_per_s": dist.sum(outer + inner) * ncell / (ms_max / 1e3),
+        "outer_cell_iters_per_s": dist.sum(outer) * ncell / (ms_max / 1e3),
         "wall_s": wall,
         "e2e": {"value": e2e_value, "unit": "cell-iters/s",
                 "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": nbytes,
@@ -314,6 +322,71 @@ def run_ours(args, dist):
     return out
 
 
+# algorithmic bytes per interior cell of each entry point's kernels: the
+# fields the reference kernel reads and writes, each once, FP64
+KERNEL_BYTES = {
+    "tea_leaf_cg_solve_calc_w": 32,       # r p Kx Ky, w w
+    "tea_leaf_cg_solve_calc_ur": {"jac_diag": 64, "jac_block": 88, "none": 56},
+    "tea_leaf_cg_solve_calc_p": 24,       # r z p, w p
+    "tea_leaf_calc_2norm": 16,
+    "tea_leaf_ppcg_solve_update_r": 56,   # r u r Kx Ky sd, w u r
+    "tea_leaf_ppcg_solve_calc_sd": {"jac_diag": 32, "jac_block": 56, "none": 24},
+    "tea_leaf_cheby_solve_calc_p": {"jac_diag": 80, "jac_block": 96, "none": 72},
+    "tea_leaf_cheby_solve_calc_u": 24,
+}
+
+
+def run_kernels(args):
+    """Each hot entry point called repeatedly on the workload's grid; every
+    kernel timed with CUDA events (non-serialising)."""
+    import ctypes
+    from tealeaf_opencl_gb300 import decks, lib
+    L = lib.load()
+    name = args.workload
+    cells, solver, prec, halo = WORKLOADS[name][:4]
+    ch = lib.Chunk(cells, cells, halo, "ppcg", prec)
+    ch.set_arithmetic(ARITHMETIC == "fused")
+    decks.setup_five_state(ch, cells)
+    ch.common_init(1, 0.004)
+    ch.calc_residual()
+    reps = args.reps
+    L.tea_gb300_kernel_timer_select(b"*")
+    rro = ch.cg_init()
+    for _ in range(reps):
+        pw = ch.cg_calc_w()
+        rrn = ch.cg_calc_ur(rro / pw)
+        ch.cg_calc_p(rrn / rro)
+        rro = rrn
+        ch.calc_2norm(2)
+    a, b_, theta = decks.chebyshev_coefficients(1.0, 60.0, reps + 1)
+    ch.ppcg_init(a, b_, theta)
+    ch.ppcg_init_sd()
+    for s in range(1, reps + 1):
+        ch.ppcg_inner(s)
+    ch.cheby_init(a, b_, theta)
+    for s in range(1, reps + 1):
+        ch.cheby_iterate(s)
+    L.tea_gb300_synchronize()
+    peak, kind = measured_peak_hbm()
+    ncell = cells * cells
+    out = {"mode": "kernels", "workload": name, "cells": ncell, "reps": reps,
+           "arithmetic": ARITHMETIC, "peak_gbs": peak, "peak_kind": kind,
+           "fp64_fma_per_s": L.tea_gb300_fp64_rate(), "kernels": {}}
+    for kname, per in KERNEL_BYTES.items():
+        ms, n = ctypes.c_double(), ctypes.c_longlong()
+        L.tea_gb300_kernel_timer_read_name(kname.encode(), ctypes.byref(ms), ctypes.byref(n))
+        if not n.value:
+            continue
+        bpc = per[prec] if isinstance(per, dict) else per
+        avg = ms.value / n.value
+        gbs = bpc * ncell / (avg / 1e3) / 1e9
+        out["kernels"][kname] = {"launches": n.value, "avg_us": 1e3 * avg,
+                                 "bytes_per_cell": bpc, "achieved_gbs": gbs,
+                                 "frac": gbs / peak}
+    L.tea_gb300_kernel_timer_select(b"")
+    return out
+
+
 def cpu_sample(name, steps_timed, cap):
     """Oracle on the same deck: one warm-up step, then steps_timed steps,
     every step capped at `cap` outer iterations; returns (value, detail)."""
@@ -321,7 +394,7 @@ def cpu_sample(name, steps_timed, cap):
     cells = WORKLOADS[name][0]
     deck = deck_for(name, 1 + steps_timed)
     res = oracle.run_deck(deck, max_solver_iters=cap)
-    its = sum(res.iterations[1:1 + steps_timed])
+    its = sum(res.iterations[1:1 + steps_timed]) + sum(res.inner_iterations[1:1 + steps_timed])
     secs = sum(res.step_seconds[1:1 + steps_timed])
     return its * cells * cells / secs, {
         "iterations": its, "seconds": secs,
@@ -339,7 +412,7 @@ def run_reference(args, dist):
     res = oracle.run_deck(deck, max_solver_iters=cap)
     wall = time.perf_counter() - t0
     w, k = args.warmup, args.steps
-    its = sum(res.iterations[w:w + k])
+    its = sum(res.iterations[w:w + k]) + sum(res.inner_iterations[w:w + k])
     secs = sum(res.step_seconds[w:w + k])
     value = its * cells * cells / secs
     threads = oracle.lib().oracle_num_threads()
@@ -368,9 +441,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ppcg4096", choices=sorted(WORKLOADS))
-    ap.add_argument("--cpu-cap", type=int, default=12,
-                    help="outer iterations per CPU sample step")
+    ap.add_argument("--cpu-cap", type=int, default=24,
+                    help="outer iterations per CPU sample step (must exceed the "
+                         "CG steps before the switch for PPCG/Chebyshev)")
+    ap.add_argument("--cap", type=int, default=0,
+                    help="limit solver iterations per GPU step (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="run", choices=["run", "kernels"],
+                    help="kernels: time each hot entry point on the workload's grid")
+    ap.add_argument("--reps", type=int, default=20)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
@@ -384,6 +463,10 @@ def main():
             return
         out = run_reference(args, _Solo())
         print(json.dumps(out))
+        return
+
+    if args.mode == "kernels":
+        print(json.dumps(run_kernels(args)))
         return
 
     dist = Dist()

@@ -196,6 +196,16 @@ void ocl_unpack_buffers_(int* fields, int* offsets, int* depth, int* face,
 int tea_gb300_configure(int halo_depth, int solver, int preconditioner,
                         int profiler_on);
 
+/* Arithmetic form of the solver kernels.  1 (default): the reference's
+ * expressions with each multiply feeding an add contracted into a fused
+ * multiply-add, dot products accumulated with fused multiply-adds, and the
+ * block-Jacobi strip's first division done with a stored reciprocal.
+ * 0: every expression exactly as the reference writes it.  Applies to the
+ * current chunk and to chunks created later; set it before
+ * tea_leaf_common_init_kernel_ocl_.  Returns 0. */
+int tea_gb300_set_arithmetic(int fused);
+int tea_gb300_get_arithmetic(void);
+
 /* 1 (default): fatal errors abort; 0: record and return. */
 void tea_gb300_set_abort_on_error(int abort_on_error);
 
@@ -234,11 +244,19 @@ int tea_gb300_event_record(int slot);
 float tea_gb300_event_elapsed_ms(int start_slot, int end_slot);
 
 /* Times every launch of the kernel with the given name (as listed by
- * print_opencl_profiling_info_) with CUDA events on the library's stream,
- * without serialising other work.  Selecting resets the totals; NULL or ""
- * stops timing.  Read returns the summed milliseconds and launch count. */
+ * print_opencl_profiling_info_), or of every kernel for "*", with CUDA
+ * events on the library's stream, without serialising other work.
+ * Selecting resets the totals; NULL or "" stops timing.  Read returns the
+ * summed milliseconds and launch count of everything timed, or of one
+ * kernel name. */
 int tea_gb300_kernel_timer_select(const char* name);
 int tea_gb300_kernel_timer_read(double* total_ms, long long* launches);
+int tea_gb300_kernel_timer_read_name(const char* name, double* total_ms,
+                                     long long* launches);
+
+/* Measures the FP64 pipe: fused multiply-add instructions per second of the
+ * current GPU (independent chains, all SMs).  Needs an initialised chunk. */
+double tea_gb300_fp64_rate(void);
 
 /* Waits for all work queued on the library's stream. */
 int tea_gb300_synchronize(void);

@@ -80,6 +80,9 @@ def lib():
             "oracle_read_field_padded": (i, [i, pd, C.c_long]),
             "oracle_write_field_padded": (i, [i, pd, C.c_long]),
             "oracle_reduce": (d, [pd, i, i]),
+            "oracle_reduce_pairs": (d, [pd, pd, i, i, i]),
+            "oracle_set_arithmetic": (None, [i]),
+            "oracle_get_arithmetic": (i, []),
             "oracle_reduction_rows": (i, [i, i]),
             "oracle_run_deck": (i, [C.c_char_p, C.c_char_p, i,
                                     C.POINTER(OracleResult), C.c_char_p, i]),
@@ -114,6 +117,12 @@ def reduce(contrib):
     return lib().oracle_reduce(_pd(a), a.shape[1], a.shape[0])
 
 
+def reduce_pairs(a, b, fused):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    return lib().oracle_reduce_pairs(_pd(a), _pd(b), a.shape[1], a.shape[0], int(fused))
+
+
 class Chunk:
     """Per-call access to the oracle chunk, mirroring the C-ABI entry points."""
 
@@ -122,6 +131,9 @@ class Chunk:
         if rc != 0:
             raise RuntimeError("oracle_initialise failed %d" % rc)
         self.x_max, self.y_max, self.halo = x_max, y_max, halo
+
+    def set_arithmetic(self, fused):
+        lib().oracle_set_arithmetic(1 if fused else 0)
 
     # -- the same entry points as tealeaf_opencl_gb300.lib.Chunk -------------
     def initialise_chunk(self, xmin, ymin, dx, dy):

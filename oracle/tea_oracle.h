@@ -108,6 +108,14 @@ int oracle_write_field_padded(int field, const double* in, long n);
 
 /* the canonical fixed-order sum of an interior-sized array */
 double oracle_reduce(const double* contrib, int x_max, int y_max);
+/* the same order for a dot product: lanes accumulate acc + a*b
+ * (fused: fma(a, b, acc)) */
+double oracle_reduce_pairs(const double* a, const double* b, int x_max,
+                           int y_max, int fused);
+
+/* arithmetic form: 0 exact reference expressions, 1 fused multiply-adds */
+void oracle_set_arithmetic(int fused);
+int oracle_get_arithmetic(void);
 int oracle_reduction_rows(int x_max, int y_max);
 
 /* ---- whole runs (restatement of the Fortran driver) ---- */

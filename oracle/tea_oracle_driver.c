@@ -45,6 +45,7 @@ typedef struct {
   int halo_depth;
   int test_problem;
   int verbose;
+  int fused; /* tl_arithmetic: 0 exact, 1 fused (default) */
   int number_of_states;
   double s_density[MAX_STATES], s_energy[MAX_STATES];
   double s_xmin[MAX_STATES], s_xmax[MAX_STATES], s_ymin[MAX_STATES],
@@ -182,6 +183,7 @@ static int parse_deck(const char* text, Deck* D, char* err, int errlen) {
   D->ppcg_inner_steps = -1;
   D->solver = ORC_SOLVER_JACOBI;
   D->halo_depth = 1;
+  D->fused = 1;
 
   Lines L = deck_lines(text);
   int state_max = 0, ok = 1;
@@ -250,6 +252,17 @@ static int parse_deck(const char* text, Deck* D, char* err, int errlen) {
         }
       }
       else if (!strcmp(w, "verbose_on")) D->verbose = 1;
+      else if (!strcmp(w, "tl_arithmetic")) {
+        /* not a reference key: which arithmetic form to use */
+        const char* v = next_word(&W);
+        if (!strcmp(v, "exact")) D->fused = 0;
+        else if (!strcmp(v, "fused")) D->fused = 1;
+        else {
+          free(line);
+          free_lines(&L);
+          return perr(err, errlen, "read_input: tl_arithmetic must be exact or fused");
+        }
+      }
       else if (!strcmp(w, "tl_use_jacobi")) D->solver = ORC_SOLVER_JACOBI;
       else if (!strcmp(w, "tl_use_cg")) D->solver = ORC_SOLVER_CG;
       else if (!strcmp(w, "tl_use_ppcg")) D->solver = ORC_SOLVER_PPCG;
@@ -709,6 +722,7 @@ int oracle_run_deck(const char* deck_text, const char* log_path,
   R.max_iters_cap = max_solver_iters;
   if (log_path) R.log = fopen(log_path, "w");
 
+  oracle_set_arithmetic(D->fused);
   /* start.f90:24-115 */
   R.time = 0.0;
   R.step = 0;

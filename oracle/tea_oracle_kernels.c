@@ -39,10 +39,21 @@ typedef struct {
   int n_coefs;
   double theta_cheby, theta_ppcg;
   double *scratch[4];
+  double *scratchb[4];
 } OrcChunk;
 
 static OrcChunk C;
 static int C_ready = 0;
+
+/* Arithmetic form, as in the CUDA library: 0 = every expression of the
+ * reference kernels as written (each multiply and add rounded); 1 = the same
+ * expressions with each multiply feeding an add contracted into one fused
+ * multiply-add (C fma()), dot-product accumulation acc = fma(a,b,acc), and
+ * the block-Jacobi first-row division done through a stored reciprocal. */
+static int FUSED = 1;
+
+void oracle_set_arithmetic(int fused) { FUSED = fused ? 1 : 0; }
+int oracle_get_arithmetic(void) { return FUSED; }
 
 #define IDX(col, row) ((long)(col) + (long)(row) * C.xs)
 
@@ -87,7 +98,14 @@ static double sum8(const double* v8) {
   return butterfly32(a);
 }
 
-double oracle_reduce(const double* contrib, int X, int Y) {
+/* Lane accumulation: acc + a*b, fused or not.  Plain sums pass b = 1.0,
+ * for which both forms give acc + a exactly. */
+static inline double lane_acc(double acc, double a, double b, int fused) {
+  return fused ? fma(a, b, acc) : acc + a * b;
+}
+
+static double reduce_pairs(const double* A, const double* B, int X, int Y,
+                           int fused) {
   const int TH = oracle_reduction_rows(X, Y);
   const long ntx = (X + 31) / 32;
   const long nty = (Y + TH - 1) / TH;
@@ -110,8 +128,10 @@ double oracle_reduce(const double* contrib, int X, int Y) {
         double acc = 0.0;
         for (int j = 0; j < TH; j++) {
           const long row = (long)TH * sy + j;
-          const double v = (col < X && row < Y) ? contrib[row * X + col] : 0.0;
-          acc = acc + v;
+          const int in = col < X && row < Y;
+          const double a = in ? A[row * X + col] : 0.0;
+          const double b = in ? (B ? B[row * X + col] : 1.0) : 0.0;
+          acc = lane_acc(acc, a, b, fused);
         }
         lanes[l] = acc;
       }
@@ -131,13 +151,34 @@ double oracle_reduce(const double* contrib, int X, int Y) {
   return sum8(w8);
 }
 
-/* sum of an interior-indexed scratch array */
+double oracle_reduce(const double* contrib, int X, int Y) {
+  return reduce_pairs(contrib, NULL, X, Y, 0);
+}
+
+double oracle_reduce_pairs(const double* a, const double* b, int X, int Y,
+                           int fused) {
+  return reduce_pairs(a, b, X, Y, fused);
+}
+
+/* plain sum of an interior-indexed scratch array */
 static double reduce_scratch(int k) {
-  return oracle_reduce(C.scratch[k], C.x_max, C.y_max);
+  return reduce_pairs(C.scratch[k], NULL, C.x_max, C.y_max, 0);
+}
+
+/* dot-product sum of scratch pairs (a in scratch, b in scratchb) */
+static double reduce_dot(int k) {
+  return reduce_pairs(C.scratch[k], C.scratchb[k], C.x_max, C.y_max, FUSED);
 }
 
 #define SCR(k, col, row) \
   C.scratch[k][(long)((row)-C.H) * C.x_max + ((col)-C.H)]
+#define SCRB(k, col, row) \
+  C.scratchb[k][(long)((row)-C.H) * C.x_max + ((col)-C.H)]
+#define DOT(k, col, row, a, b) \
+  do {                         \
+    SCR(k, col, row) = (a);    \
+    SCRB(k, col, row) = (b);   \
+  } while (0)
 
 /* ------------------------------------------------------------------------ */
 /* Lifecycle                                                                */
@@ -155,7 +196,8 @@ void oracle_finalise(void) {
                     &C.vertexy, &C.vertexdy, &C.p, &C.r, &C.w, &C.Mi, &C.Kx,
                     &C.Ky, &C.sd, &C.u, &C.u0, &C.z, &C.cp, &C.bfp,
                     &C.ch_alphas, &C.ch_betas, &C.ztmp, &C.scratch[0], &C.scratch[1],
-                    &C.scratch[2], &C.scratch[3]};
+                    &C.scratch[2], &C.scratch[3], &C.scratchb[0], &C.scratchb[1],
+                    &C.scratchb[2], &C.scratchb[3]};
   for (size_t i = 0; i < sizeof(all) / sizeof(all[0]); i++) {
     free(*all[i]);
     *all[i] = NULL;
@@ -191,7 +233,8 @@ int oracle_initialise(int x_max, int y_max, int H, int solver, int prec) {
   }
   for (int k = 0; k < 4; k++) {
     C.scratch[k] = zalloc((long)x_max * y_max);
-    if (!C.scratch[k]) return -2;
+    C.scratchb[k] = zalloc((long)x_max * y_max);
+    if (!C.scratch[k] || !C.scratchb[k]) return -2;
   }
   C_ready = 1;
   return 0;
@@ -293,9 +336,18 @@ void oracle_set_field(void) {
  * tea_leaf_cg_cl.cl:59-63. */
 static inline double smvp_at(const double* x, long c) {
   const long xs = C.xs;
-  return (1.0 + (C.Ky[c + xs] + C.Ky[c]) + (C.Kx[c + 1] + C.Kx[c])) * x[c] -
-         (C.Ky[c + xs] * x[c + xs] + C.Ky[c] * x[c - xs]) -
-         (C.Kx[c + 1] * x[c + 1] + C.Kx[c] * x[c - 1]);
+  const double D = (1.0 + (C.Ky[c + xs] + C.Ky[c]) + (C.Kx[c + 1] + C.Kx[c]));
+  if (!FUSED)
+    return D * x[c] - (C.Ky[c + xs] * x[c + xs] + C.Ky[c] * x[c - xs]) -
+           (C.Kx[c + 1] * x[c + 1] + C.Kx[c] * x[c - 1]);
+  const double t1 = fma(C.Ky[c], x[c - xs], C.Ky[c + xs] * x[c + xs]);
+  const double t2 = fma(C.Kx[c], x[c - 1], C.Kx[c + 1] * x[c + 1]);
+  return fma(D, x[c], -t1) - t2;
+}
+
+/* a*p + bl*br, the Chebyshev/PPCG coefficient update */
+static inline double coef_update(double a, double p, double bl, double br) {
+  return FUSED ? fma(a, p, bl * br) : a * p + bl * br;
 }
 
 /* Rows in the 4-row block-Jacobi strip starting at interior row 4g:
@@ -326,6 +378,7 @@ static void block_init(void) {
     const int upper = block_top(g);
     for (int col = H; col < H + C.x_max; col++) {
       C.cp[IDX(col, row0)] = COEF_C(row0) / COEF_B(row0);
+      if (FUSED) C.bfp[IDX(col, row0)] = 1.0 / COEF_B(row0);
       for (int k = 1; k < upper; k++) {
         const int rk = row0 + k;
         C.bfp[IDX(col, rk)] =
@@ -353,14 +406,18 @@ static void block_solve(const double* rin, double* zout) {
         const int rk = row0 + k;
         rl[k] = (rk < H + C.y_max) ? rin[IDX(col, rk)] : 0.0;
       }
-      dp[0] = rl[0] / COEF_B(row0);
+      dp[0] = FUSED ? rl[0] * C.bfp[IDX(col, row0)] : rl[0] / COEF_B(row0);
       for (int k = 1; k < upper; k++) {
         const int rk = row0 + k;
-        dp[k] = (rl[k] - COEF_A(rk) * dp[k - 1]) * C.bfp[IDX(col, rk)];
+        if (FUSED)
+          dp[k] = fma(C.Ky[IDX(col, rk)], dp[k - 1], rl[k]) * C.bfp[IDX(col, rk)];
+        else
+          dp[k] = (rl[k] - COEF_A(rk) * dp[k - 1]) * C.bfp[IDX(col, rk)];
       }
       zl[upper - 1] = dp[upper - 1];
       for (int k = upper - 2; k >= 0; k--)
-        zl[k] = dp[k] - C.cp[IDX(col, row0 + k)] * zl[k + 1];
+        zl[k] = FUSED ? fma(-C.cp[IDX(col, row0 + k)], zl[k + 1], dp[k])
+                      : dp[k] - C.cp[IDX(col, row0 + k)] * zl[k + 1];
       for (int k = 0; k < upper; k++) {
         const int rk = row0 + k;
         if (rk < H + C.y_max) zout[IDX(col, rk)] = zl[k];
@@ -477,9 +534,9 @@ void oracle_calc_2norm(int which, double* norm) {
   for (int row = H; row < H + C.y_max; row++)
     for (int col = H; col < H + C.x_max; col++) {
       const long c = IDX(col, row);
-      SCR(0, col, row) = a[c] * b[c];
+      DOT(0, col, row, a[c], b[c]);
     }
-  *norm = reduce_scratch(0);
+  *norm = reduce_dot(0);
 }
 
 /* tea_leaf_init_jac_diag, tea_leaf_common_cl.cl:127-142, whole array */
@@ -516,9 +573,9 @@ void oracle_cg_init(double* rro) {
       } else {
         C.p[c] = C.r[c];
       }
-      SCR(0, col, row) = C.r[c] * C.p[c];
+      DOT(0, col, row, C.r[c], C.p[c]);
     }
-  *rro = reduce_scratch(0);
+  *rro = reduce_dot(0);
 }
 
 /* tea_leaf_cg_solve_calc_w, tea_leaf_cg_cl.cl:45-69 */
@@ -529,9 +586,9 @@ void oracle_cg_calc_w(double* pw) {
     for (int col = H; col < H + C.x_max; col++) {
       const long c = IDX(col, row);
       C.w[c] = smvp_at(C.p, c);
-      SCR(0, col, row) = C.p[c] * C.w[c];
+      DOT(0, col, row, C.p[c], C.w[c]);
     }
-  *pw = reduce_scratch(0);
+  *pw = reduce_dot(0);
 }
 
 /* tea_leaf_cg_solve_calc_ur, tea_leaf_cg_cl.cl:73-137 */
@@ -541,8 +598,13 @@ void oracle_cg_calc_ur(double alpha, double* rrn) {
   for (int row = H; row < H + C.y_max; row++)
     for (int col = H; col < H + C.x_max; col++) {
       const long c = IDX(col, row);
-      C.u[c] = C.u[c] + alpha * C.p[c];
-      C.r[c] = C.r[c] - alpha * C.w[c];
+      if (FUSED) {
+        C.u[c] = fma(alpha, C.p[c], C.u[c]);
+        C.r[c] = fma(-alpha, C.w[c], C.r[c]);
+      } else {
+        C.u[c] = C.u[c] + alpha * C.p[c];
+        C.r[c] = C.r[c] - alpha * C.w[c];
+      }
     }
   if (C.prec == ORC_PREC_JAC_BLOCK) block_solve(C.r, C.z);
 #pragma omp parallel for schedule(static)
@@ -550,15 +612,15 @@ void oracle_cg_calc_ur(double alpha, double* rrn) {
     for (int col = H; col < H + C.x_max; col++) {
       const long c = IDX(col, row);
       if (C.prec == ORC_PREC_JAC_BLOCK) {
-        SCR(0, col, row) = C.r[c] * C.z[c];
+        DOT(0, col, row, C.r[c], C.z[c]);
       } else if (C.prec == ORC_PREC_JAC_DIAG) {
         C.z[c] = C.r[c] * C.Mi[c];
-        SCR(0, col, row) = C.r[c] * C.z[c];
+        DOT(0, col, row, C.r[c], C.z[c]);
       } else {
-        SCR(0, col, row) = C.r[c] * C.r[c];
+        DOT(0, col, row, C.r[c], C.r[c]);
       }
     }
-  *rrn = reduce_scratch(0);
+  *rrn = reduce_dot(0);
 }
 
 /* tea_leaf_cg_solve_calc_p, tea_leaf_cg_cl.cl:141-160 */
@@ -568,10 +630,8 @@ void oracle_cg_calc_p(double beta) {
   for (int row = H; row < H + C.y_max; row++)
     for (int col = H; col < H + C.x_max; col++) {
       const long c = IDX(col, row);
-      if (C.prec != ORC_PREC_NONE)
-        C.p[c] = C.z[c] + beta * C.p[c];
-      else
-        C.p[c] = C.r[c] + beta * C.p[c];
+      const double src = (C.prec != ORC_PREC_NONE) ? C.z[c] : C.r[c];
+      C.p[c] = FUSED ? fma(beta, C.p[c], src) : src + beta * C.p[c];
     }
 }
 
@@ -649,11 +709,11 @@ void oracle_cheby_iterate(int step) {
     for (int col = H; col < H + C.x_max; col++) {
       const long c = IDX(col, row);
       if (C.prec == ORC_PREC_JAC_BLOCK)
-        C.p[c] = a * C.p[c] + b * C.ztmp[c];
+        C.p[c] = coef_update(a, C.p[c], b, C.ztmp[c]);
       else if (C.prec == ORC_PREC_JAC_DIAG)
-        C.p[c] = a * C.p[c] + b * C.Mi[c] * C.r[c];
+        C.p[c] = coef_update(a, C.p[c], b * C.Mi[c], C.r[c]);
       else
-        C.p[c] = a * C.p[c] + b * C.r[c];
+        C.p[c] = coef_update(a, C.p[c], b, C.r[c]);
     }
   cheby_calc_u();
 }
@@ -714,11 +774,11 @@ void oracle_ppcg_inner(int step) {
     for (int col = H; col < H + C.x_max; col++) {
       const long c = IDX(col, row);
       if (C.prec == ORC_PREC_JAC_BLOCK)
-        C.sd[c] = a * C.sd[c] + b * zl[c];
+        C.sd[c] = coef_update(a, C.sd[c], b, zl[c]);
       else if (C.prec == ORC_PREC_JAC_DIAG)
-        C.sd[c] = a * C.sd[c] + b * C.r[c] * C.Mi[c];
+        C.sd[c] = coef_update(a, C.sd[c], b * C.r[c], C.Mi[c]);
       else
-        C.sd[c] = a * C.sd[c] + b * C.r[c];
+        C.sd[c] = coef_update(a, C.sd[c], b, C.r[c]);
     }
 }
 

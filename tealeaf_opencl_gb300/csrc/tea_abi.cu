@@ -67,14 +67,15 @@ struct ProfEntry {
 static std::map<std::string, ProfEntry> g_prof;
 static cudaEvent_t g_prof_ev[2] = {nullptr, nullptr};
 
-// Optional timing of one named kernel inside a running workload: event
-// pairs recorded around each of its launches on the library's stream, read
-// back in batches without serialising the other work.
+// Optional timing of kernels inside a running workload: event pairs
+// recorded around each launch on the library's stream and read back in
+// batches, without serialising the other work.  The selection is one kernel
+// name, or "*" for every kernel.
 static std::string g_timed_name;
 static std::vector<cudaEvent_t> g_timed_ev;
+static std::vector<std::string> g_timed_names;
 static size_t g_timed_used = 0;
-static double g_timed_ms = 0.0;
-static long long g_timed_n = 0;
+static std::map<std::string, ProfEntry> g_timed;
 
 static void timed_drain() {
   if (g_timed_used == 0) return;
@@ -82,20 +83,27 @@ static void timed_drain() {
   for (size_t i = 0; i < g_timed_used; i++) {
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, g_timed_ev[2 * i], g_timed_ev[2 * i + 1]);
-    g_timed_ms += ms;
-    g_timed_n++;
+    ProfEntry& e = g_timed[g_timed_names[i]];
+    e.ms += ms;
+    e.calls++;
   }
   g_timed_used = 0;
 }
 
+static bool timed_match(const char* name) {
+  return !g_timed_name.empty() && (g_timed_name == "*" || g_timed_name == name);
+}
+
 void profile_begin(const char* name) {
   Chunk& c = chunk();
-  if (!g_timed_name.empty() && g_timed_name == name) {
+  if (timed_match(name)) {
     if (g_timed_ev.empty()) {
       g_timed_ev.resize(2 * 1024);
+      g_timed_names.resize(1024);
       for (auto& e : g_timed_ev) cudaEventCreate(&e);
     }
     if (2 * (g_timed_used + 1) > g_timed_ev.size()) timed_drain();
+    g_timed_names[g_timed_used] = name;
     cudaEventRecord(g_timed_ev[2 * g_timed_used], c.stream);
   }
   if (!c.profiler_on) return;
@@ -110,7 +118,7 @@ void profile_begin(const char* name) {
 // (ocl_errors.cpp:75-122).
 void profile_end(const char* name) {
   Chunk& c = chunk();
-  if (!g_timed_name.empty() && g_timed_name == name) {
+  if (timed_match(name)) {
     cudaEventRecord(g_timed_ev[2 * g_timed_used + 1], c.stream);
     g_timed_used++;
   }
@@ -165,6 +173,7 @@ Dev Chunk::dev() const {
   d.z = z.f;
   d.cp = cp.f;
   d.bfp = bfp.f;
+  d.diag = diag.f;
   d.un = Mi.f;  // the reference reuses vector_Mi as Jacobi's un
   d.cellx = cellx;
   d.celly = celly;
@@ -191,7 +200,7 @@ static void free_chunk(Chunk& c) {
   resident_release();
   Field* l[] = {&c.density, &c.energy0, &c.energy1, &c.volume, &c.u, &c.u0,
                 &c.p,       &c.r,       &c.w,       &c.Mi,     &c.Kx, &c.Ky,
-                &c.sd,      &c.z,       &c.cp,      &c.bfp};
+                &c.sd,      &c.z,       &c.cp,      &c.bfp,    &c.diag};
   for (Field* f : l) {
     cudaFree(f->base);
     f->base = f->f = nullptr;
@@ -233,6 +242,7 @@ static bool alloc_field(Chunk& c, Field& f) {
 struct Config {
   bool set = false;
   int halo = 1, solver = SOLVER_JACOBI, prec = PREC_NONE, profiler = 0;
+  int fused = 1;
 };
 static Config g_config;
 
@@ -306,6 +316,7 @@ static bool init_chunk(int x_max, int y_max, const Config& cfg) {
   c.solver = cfg.solver;
   c.prec = cfg.prec;
   c.profiler_on = cfg.profiler != 0;
+  c.fused = cfg.fused != 0;
   c.TH = reduction_rows(x_max, y_max);
   c.S = ((long long)(x_max + 2 * c.H + 1 + 31) / 32) * 32;
   c.rows = y_max + 2 * c.H + 1;
@@ -317,7 +328,7 @@ static bool init_chunk(int x_max, int y_max, const Config& cfg) {
   c.ready = true;  // so that free_chunk releases partial allocations
   Field* l[] = {&c.density, &c.energy0, &c.energy1, &c.volume, &c.u, &c.u0,
                 &c.p,       &c.r,       &c.w,       &c.Mi,     &c.Kx, &c.Ky,
-                &c.sd,      &c.z,       &c.cp,      &c.bfp};
+                &c.sd,      &c.z,       &c.cp,      &c.bfp,    &c.diag};
   for (Field* f : l)
     if (!alloc_field(c, *f)) return false;
   const int n1 = std::max(x_max, y_max) + 2 * c.H + 2;
@@ -508,6 +519,7 @@ extern "C" void tea_leaf_common_init_kernel_ocl_(const int* coefficient,
   *ry = *dt / (dy * dy);
   launch_init_common(c, *coefficient, *rx, *ry);
   if (!*reflective_boundary) launch_zero_boundary(c, zero_boundary);
+  launch_init_diag(c);
   launch_init_u(c, c.energy1.f);
 }
 
@@ -716,6 +728,14 @@ extern "C" int tea_gb300_configure(int halo_depth, int solver,
 
 extern "C" void tea_gb300_set_abort_on_error(int a) { g_abort_on_error = a; }
 
+extern "C" int tea_gb300_set_arithmetic(int fused) {
+  g_config.fused = fused ? 1 : 0;
+  chunk().fused = fused != 0;
+  return 0;
+}
+
+extern "C" int tea_gb300_get_arithmetic(void) { return chunk().fused ? 1 : 0; }
+
 extern "C" int tea_gb300_last_error(char* msg, int len) {
   const int code = g_err_code;
   if (msg && len > 0) {
@@ -751,6 +771,8 @@ static int copy_field(int id, double* host, const double* in, bool padded) {
                           w * sizeof(double), h, cudaMemcpyDeviceToHost,
                           c.stream);
   if (!check_cuda(e, "field copy")) return -1;
+  // the stored diagonal follows the face coefficients
+  if (in && (id == 12 || id == 13)) launch_init_diag(c);
   return check_cuda(cudaStreamSynchronize(c.stream), "field copy sync") ? 0 : -1;
 }
 
@@ -822,14 +844,30 @@ extern "C" void tea_gb300_host_free(void* p) { cudaFreeHost(p); }
 extern "C" int tea_gb300_kernel_timer_select(const char* name) {
   timed_drain();
   g_timed_name = name ? name : "";
-  g_timed_ms = 0.0;
-  g_timed_n = 0;
+  g_timed.clear();
   return 0;
 }
 
 extern "C" int tea_gb300_kernel_timer_read(double* total_ms, long long* launches) {
   timed_drain();
-  *total_ms = g_timed_ms;
-  *launches = g_timed_n;
+  double ms = 0.0;
+  long long n = 0;
+  for (auto& kv : g_timed) {
+    ms += kv.second.ms;
+    n += kv.second.calls;
+  }
+  *total_ms = ms;
+  *launches = n;
   return 0;
 }
+
+extern "C" int tea_gb300_kernel_timer_read_name(const char* name, double* total_ms,
+                                                long long* launches) {
+  timed_drain();
+  auto it = g_timed.find(name ? name : "");
+  *total_ms = it == g_timed.end() ? 0.0 : it->second.ms;
+  *launches = it == g_timed.end() ? 0 : it->second.calls;
+  return 0;
+}
+
+extern "C" double tea_gb300_fp64_rate(void) { return measure_fp64_rate(); }

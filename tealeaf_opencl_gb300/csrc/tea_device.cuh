@@ -19,6 +19,19 @@
 //      sums as in 3.
 // All arithmetic is compiled with --fmad=false, so every operation rounds
 // exactly as written.
+//
+// Two arithmetic forms, chosen per chunk (template parameter F):
+//   exact (F = false): every expression of the reference kernels as written,
+//     each multiply and add rounded separately;
+//   fused (F = true): the same expressions with each multiply feeding an add
+//     contracted into one fused multiply-add (what OpenCL's default
+//     FP_CONTRACT allows a GPU compiler to do), and the per-strip division of
+//     the block-Jacobi solve replaced by a multiply with the reciprocal kept
+//     in bfp at the strip's first row.
+// The diagonal 1 + (Ky_n + Ky_c) + (Kx_e + Kx_c) is precomputed once per
+// timestep into d.diag with the reference's association, so using it is
+// bit-identical to recomputing it.  GB300's FP64 pipe, not HBM, bounds these
+// kernels, and the fused form roughly halves their FP64 instruction count.
 #pragma once
 
 #include "tea_internal.h"
@@ -38,14 +51,28 @@ __device__ __forceinline__ double bfly(double v) {
 }
 
 // The 5-point operator in the association every reference kernel uses
-// (e.g. tea_leaf_cg_cl.cl:59-63).
+// (e.g. tea_leaf_cg_cl.cl:59-63):
+//   (1 + (Ky_n + Ky_c) + (Kx_e + Kx_c)) x_c - (Ky_n x_n + Ky_c x_s)
+//                                           - (Kx_e x_e + Kx_c x_w)
+template <bool F>
 __device__ __forceinline__ double smvp(const Dev& d, const double* x,
                                        long long c) {
   const long long S = d.S;
   const double kyn = __ldg(d.Ky + c + S), kyc = __ldg(d.Ky + c);
   const double kxe = __ldg(d.Kx + c + 1), kxc = __ldg(d.Kx + c);
-  return (1.0 + (kyn + kyc) + (kxe + kxc)) * x[c] -
-         (kyn * x[c + S] + kyc * x[c - S]) - (kxe * x[c + 1] + kxc * x[c - 1]);
+  const double D = __ldg(d.diag + c);
+  if (!F)
+    return D * x[c] - (kyn * x[c + S] + kyc * x[c - S]) -
+           (kxe * x[c + 1] + kxc * x[c - 1]);
+  const double t1 = __fma_rn(kyc, x[c - S], kyn * x[c + S]);
+  const double t2 = __fma_rn(kxc, x[c - 1], kxe * x[c + 1]);
+  return __fma_rn(D, x[c], -t1) - t2;
+}
+
+// acc + a*b of the per-lane dot-product accumulation
+template <bool F>
+__device__ __forceinline__ double accum(double acc, double a, double b) {
+  return F ? __fma_rn(a, b, acc) : acc + a * b;
 }
 
 // COEF_B of the block-Jacobi strip (tea_block_jacobi.cl:3) at offset c.
@@ -63,35 +90,48 @@ __device__ __forceinline__ int strip_rows(const Dev& d, int y) {
   return up < 4 ? up : 4;
 }
 
+// One forward step of the strip's Thomas algorithm:
+// (r - COEF_A dp) * bfp with COEF_A = -Ky
+template <bool F>
+__device__ __forceinline__ double fwd(double r, double ky, double dp,
+                                      double bfp) {
+  return F ? __fma_rn(ky, dp, r) * bfp : (r - (-ky) * dp) * bfp;
+}
+
+// One back-substitution step: dp - cp z
+template <bool F>
+__device__ __forceinline__ double bwd(double dp, double cp, double z) {
+  return F ? __fma_rn(-cp, z, dp) : dp - cp * z;
+}
+
 // block_solve_func (tea_block_jacobi.cl:6-42) for one column of one strip:
 // z = M_block^-1 r for the strip whose first cell is at offset c0.
+template <bool F>
 __device__ __forceinline__ void strip_solve(const Dev& d, long long c0,
                                             int upper, const double rl[4],
                                             double zl[4]) {
   const long long S = d.S;
   double dp0, dp1 = 0.0, dp2 = 0.0, dp3 = 0.0;
-  dp0 = rl[0] / coef_b(d, c0);
+  dp0 = F ? rl[0] * __ldg(d.bfp + c0) : rl[0] / __ldg(d.diag + c0);
   if (upper > 1)
-    dp1 = (rl[1] - (-__ldg(d.Ky + c0 + S)) * dp0) * __ldg(d.bfp + c0 + S);
+    dp1 = fwd<F>(rl[1], __ldg(d.Ky + c0 + S), dp0, __ldg(d.bfp + c0 + S));
   if (upper > 2)
-    dp2 = (rl[2] - (-__ldg(d.Ky + c0 + 2 * S)) * dp1) *
-          __ldg(d.bfp + c0 + 2 * S);
+    dp2 = fwd<F>(rl[2], __ldg(d.Ky + c0 + 2 * S), dp1, __ldg(d.bfp + c0 + 2 * S));
   if (upper > 3)
-    dp3 = (rl[3] - (-__ldg(d.Ky + c0 + 3 * S)) * dp2) *
-          __ldg(d.bfp + c0 + 3 * S);
+    dp3 = fwd<F>(rl[3], __ldg(d.Ky + c0 + 3 * S), dp2, __ldg(d.bfp + c0 + 3 * S));
   double z0, z1 = 0.0, z2 = 0.0, z3 = 0.0;
   if (upper == 4) {
     z3 = dp3;
-    z2 = dp2 - __ldg(d.cp + c0 + 2 * S) * z3;
-    z1 = dp1 - __ldg(d.cp + c0 + S) * z2;
-    z0 = dp0 - __ldg(d.cp + c0) * z1;
+    z2 = bwd<F>(dp2, __ldg(d.cp + c0 + 2 * S), z3);
+    z1 = bwd<F>(dp1, __ldg(d.cp + c0 + S), z2);
+    z0 = bwd<F>(dp0, __ldg(d.cp + c0), z1);
   } else if (upper == 3) {
     z2 = dp2;
-    z1 = dp1 - __ldg(d.cp + c0 + S) * z2;
-    z0 = dp0 - __ldg(d.cp + c0) * z1;
+    z1 = bwd<F>(dp1, __ldg(d.cp + c0 + S), z2);
+    z0 = bwd<F>(dp0, __ldg(d.cp + c0), z1);
   } else if (upper == 2) {
     z1 = dp1;
-    z0 = dp0 - __ldg(d.cp + c0) * z1;
+    z0 = bwd<F>(dp0, __ldg(d.cp + c0), z1);
   } else {
     z0 = dp0;
   }

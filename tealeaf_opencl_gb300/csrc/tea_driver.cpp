@@ -56,6 +56,7 @@ struct Deck {
   int halo = 1;
   int test_problem = 0;
   bool verbose = false;
+  bool fused = true;  // tl_arithmetic
   std::vector<State> states;
 };
 
@@ -164,6 +165,16 @@ bool parse_deck(const std::string& text, Deck* D, std::string* err) {
         }
       }
       else if (w == "verbose_on") D->verbose = true;
+      else if (w == "tl_arithmetic") {
+        // not a reference key: the arithmetic form of the solver kernels
+        const std::string v = next();
+        if (v == "exact") D->fused = false;
+        else if (v == "fused") D->fused = true;
+        else {
+          *err = "read_input: tl_arithmetic must be exact or fused";
+          return false;
+        }
+      }
       else if (w == "tl_use_jacobi") D->solver = TEA_SOLVER_JACOBI;
       else if (w == "tl_use_cg") D->solver = TEA_SOLVER_CG;
       else if (w == "tl_use_ppcg") D->solver = TEA_SOLVER_PPCG;
@@ -398,6 +409,7 @@ class Driver {
     mode = m;
     cap = c;
     if (log_path) logfile = fopen(log_path, "w");
+    tea_gb300_set_arithmetic(D.fused ? 1 : 0);
     if (tea_gb300_configure(D.halo, D.solver, D.prec, 0) != 0) {
       *err = "invalid configuration";
       return false;

@@ -36,6 +36,7 @@ struct Dev {
   int ntx, nsx, nty, ns;  // tiling for the chunk's tile height
   double *density, *energy0, *energy1, *volume;
   double *u, *u0, *p, *r, *w, *Mi, *Kx, *Ky, *sd, *z, *cp, *bfp, *un;
+  double* diag;  // 1 + (Ky_n + Ky_c) + (Kx_e + Kx_c), set by common_init
   double *cellx, *celly, *celldx, *celldy, *vertexx, *vertexy, *vertexdx,
       *vertexdy;
 };
@@ -81,7 +82,8 @@ struct Chunk {
   int device = 0, num_sms = 0;
   cudaStream_t stream = nullptr;
   Field density, energy0, energy1, volume, u, u0, p, r, w, Mi, Kx, Ky, sd, z,
-      cp, bfp, un;
+      cp, bfp, diag;
+  bool fused = true;  // arithmetic form (see tea_device.cuh)
   double *cellx = nullptr, *celly = nullptr, *celldx = nullptr,
          *celldy = nullptr, *vertexx = nullptr, *vertexy = nullptr,
          *vertexdx = nullptr, *vertexdy = nullptr;
@@ -143,6 +145,7 @@ void launch_zero_boundary(Chunk& c, const int* zero_boundary);
 void launch_calc_residual(Chunk& c);
 void launch_dot(Chunk& c, const double* a, const double* b);
 void launch_init_jac_diag(Chunk& c);
+void launch_init_diag(Chunk& c);
 void launch_block_init(Chunk& c);
 void launch_cg_init_p(Chunk& c);
 void launch_cg_calc_w(Chunk& c);
@@ -165,5 +168,7 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
                            double* error_out, int* n_done, int* converged,
                            double* cg_alphas, double* cg_betas);
 void resident_release();
+// FP64 fused-multiply-add instructions per second of this GPU
+double measure_fp64_rate();
 
 }  // namespace tea

@@ -52,12 +52,19 @@ static void launch_2d(Chunk& c, const char* name, int nx, int ny,
   profile_end(name);
 }
 
-#define TH_DISPATCH(c, name, kern, ...)                   \
-  do {                                                    \
-    if ((c).TH == 16)                                     \
-      launch_tile(c, name, kern<16>, __VA_ARGS__);        \
-    else                                                  \
-      launch_tile(c, name, kern<4>, __VA_ARGS__);         \
+#define TH_DISPATCH(c, name, kern, ...)                       \
+  do {                                                        \
+    if ((c).TH == 16) {                                       \
+      if ((c).fused)                                          \
+        launch_tile(c, name, kern<16, true>, __VA_ARGS__);    \
+      else                                                    \
+        launch_tile(c, name, kern<16, false>, __VA_ARGS__);   \
+    } else {                                                  \
+      if ((c).fused)                                          \
+        launch_tile(c, name, kern<4, true>, __VA_ARGS__);     \
+      else                                                    \
+        launch_tile(c, name, kern<4, false>, __VA_ARGS__);    \
+    }                                                         \
   } while (0)
 
 // ---------------------------------------------------------------------------
@@ -221,7 +228,7 @@ __global__ void k_init_jac_diag(Dev d) {
 
 // tea_leaf_block_init, tea_block_jacobi.cl:78-105: one thread per column of
 // one 4-row strip
-__global__ void k_block_init(Dev d) {
+__global__ void k_block_init(Dev d, int fused) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int g = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= d.x_max || 4 * g >= d.y_max) return;
@@ -230,6 +237,9 @@ __global__ void k_block_init(Dev d) {
   const long long c0 = cidx(d, x, 4 * g);
   double cpv = (-d.Ky[c0 + S]) / coef_b(d, c0);
   d.cp[c0] = cpv;
+  // the fused form divides by COEF_B of the first row through its
+  // reciprocal, kept in the otherwise unused bfp of that row
+  if (fused) d.bfp[c0] = 1.0 / coef_b(d, c0);
   for (int k = 1; k < upper; k++) {
     const long long ck = c0 + k * S;
     const double b = 1.0 / (coef_b(d, ck) - (-d.Ky[ck]) * cpv);
@@ -262,11 +272,11 @@ __global__ void k_update_halo(Dev d, int mask, int depth) {
 }
 
 // ---------------------------------------------------------------------------
-// interior tile kernels
+// interior tile kernels (TH: reduction tile height, F: fused arithmetic)
 // ---------------------------------------------------------------------------
 
 // tea_leaf_calc_residual, tea_leaf_common_cl.cl:17-36
-template <int TH>
+template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock) k_calc_residual(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
@@ -275,7 +285,7 @@ __global__ void __launch_bounds__(kBlock) k_calc_residual(Dev d, Red red) {
       const int y = y0 + j;
       if (y < d.y_max) {
         const long long c = cidx(d, x, y);
-        const double s = smvp(d, d.u, c);
+        const double s = smvp<F>(d, d.u, c);
         d.r[c] = d.u0[c] - s;
       }
     }
@@ -283,19 +293,20 @@ __global__ void __launch_bounds__(kBlock) k_calc_residual(Dev d, Red red) {
 }
 
 // tea_leaf_calc_2norm, tea_leaf_common_cl.cl:38-54
-template <int TH>
+template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock)
     k_dot(Dev d, Red red, const double* a, const double* b) {
   tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
 #pragma unroll 4
     for (int j = 0; j < TH; j++) {
       const int y = y0 + j;
-      double v = 0.0;
+      double av = 0.0, bv = 0.0;
       if (xin && y < d.y_max) {
         const long long c = cidx(d, x, y);
-        v = a[c] * b[c];
+        av = a[c];
+        bv = b[c];
       }
-      acc[0] = acc[0] + v;
+      acc[0] = accum<F>(acc[0], av, bv);
     }
   });
 }
@@ -303,37 +314,38 @@ __global__ void __launch_bounds__(kBlock)
 // tea_leaf_block_solve (tea_block_jacobi.cl:44-76) fused with
 // tea_leaf_cg_solve_init_p (tea_leaf_cg_cl.cl:8-41): z = M^-1 r, p = z,
 // sum r.p
-template <int TH>
+template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock) k_cg_init_p(Dev d, Red red) {
   tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (d.prec == PREC_JAC_BLOCK) {
 #pragma unroll 1
       for (int ys = y0; ys < y0 + TH; ys += 4) {
-        double zl[4] = {0.0, 0.0, 0.0, 0.0}, rl[4];
+        double zl[4] = {0.0, 0.0, 0.0, 0.0}, rl[4] = {0.0, 0.0, 0.0, 0.0};
         const long long c0 = cidx(d, x, ys);
         if (xin && ys < d.y_max) {
 #pragma unroll
           for (int i = 0; i < 4; i++)
             rl[i] = (ys + i < d.y_max) ? d.r[c0 + i * d.S] : 0.0;
-          strip_solve(d, c0, strip_rows(d, ys), rl, zl);
+          strip_solve<F>(d, c0, strip_rows(d, ys), rl, zl);
         }
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-          double v = 0.0;
+          double av = 0.0, bv = 0.0;
           if (xin && ys + i < d.y_max) {
             const long long c = c0 + i * d.S;
             d.z[c] = zl[i];
             d.p[c] = zl[i];
-            v = rl[i] * zl[i];
+            av = rl[i];
+            bv = zl[i];
           }
-          acc[0] = acc[0] + v;
+          acc[0] = accum<F>(acc[0], av, bv);
         }
       }
     } else {
 #pragma unroll 4
       for (int j = 0; j < TH; j++) {
         const int y = y0 + j;
-        double v = 0.0;
+        double av = 0.0, bv = 0.0;
         if (xin && y < d.y_max) {
           const long long c = cidx(d, x, y);
           const double rv = d.r[c];
@@ -345,9 +357,10 @@ __global__ void __launch_bounds__(kBlock) k_cg_init_p(Dev d, Red red) {
             pv = rv;
           }
           d.p[c] = pv;
-          v = rv * pv;
+          av = rv;
+          bv = pv;
         }
-        acc[0] = acc[0] + v;
+        acc[0] = accum<F>(acc[0], av, bv);
       }
     }
   });
@@ -356,7 +369,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_init_p(Dev d, Red red) {
 // tea_leaf_cg_solve_calc_w, tea_leaf_cg_cl.cl:45-69.  With st != nullptr
 // (device-resident loop) it does nothing once the loop has stopped and
 // leaves pw in st.
-template <int TH>
+template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock)
     k_cg_calc_w(Dev d, Red red, ResState* st) {
   if (st && *(volatile int*)&st->stop) return;
@@ -364,17 +377,34 @@ __global__ void __launch_bounds__(kBlock)
 #pragma unroll 4
     for (int j = 0; j < TH; j++) {
       const int y = y0 + j;
-      double v = 0.0;
+      double av = 0.0, bv = 0.0;
       if (xin && y < d.y_max) {
         const long long c = cidx(d, x, y);
-        const double wv = smvp(d, d.p, c);
+        const double wv = smvp<F>(d, d.p, c);
         d.w[c] = wv;
-        v = d.p[c] * wv;
+        av = d.p[c];
+        bv = wv;
       }
-      acc[0] = acc[0] + v;
+      acc[0] = accum<F>(acc[0], av, bv);
     }
   });
   if (st && last && threadIdx.x == 0) st->pw = red.result[0];
+}
+
+// u += alpha p; r -= alpha w (tea_leaf_cg_cl.cl:88-89), returns the new r
+template <bool F>
+__device__ __forceinline__ double ur_update(const Dev& d, long long c,
+                                            double alpha) {
+  if (F) {
+    d.u[c] = __fma_rn(alpha, d.p[c], d.u[c]);
+    const double rv = __fma_rn(-alpha, d.w[c], d.r[c]);
+    d.r[c] = rv;
+    return rv;
+  }
+  d.u[c] = d.u[c] + alpha * d.p[c];
+  const double rv = d.r[c] - alpha * d.w[c];
+  d.r[c] = rv;
+  return rv;
 }
 
 // tea_leaf_cg_solve_calc_ur, tea_leaf_cg_cl.cl:73-137.  In the
@@ -382,7 +412,7 @@ __global__ void __launch_bounds__(kBlock)
 // finishes the reduction carries out the host steps of one CG iteration
 // (tea_solve.f90:282-330): beta = rrn/rro, rro = rrn, error = sqrt(rrn) and
 // the exit test against eps * initial_residual.
-template <int TH>
+template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock)
     k_cg_calc_ur(Dev d, Red red, double alpha, ResState* st) {
   if (st) {
@@ -397,46 +427,39 @@ __global__ void __launch_bounds__(kBlock)
         const long long c0 = cidx(d, x, ys);
         if (xin && ys < d.y_max) {
 #pragma unroll
-          for (int i = 0; i < 4; i++) {
-            if (ys + i < d.y_max) {
-              const long long c = c0 + i * d.S;
-              d.u[c] = d.u[c] + alpha * d.p[c];
-              const double rv = d.r[c] - alpha * d.w[c];
-              d.r[c] = rv;
-              rl[i] = rv;
-            }
-          }
-          strip_solve(d, c0, strip_rows(d, ys), rl, zl);
+          for (int i = 0; i < 4; i++)
+            if (ys + i < d.y_max) rl[i] = ur_update<F>(d, c0 + i * d.S, alpha);
+          strip_solve<F>(d, c0, strip_rows(d, ys), rl, zl);
         }
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-          double v = 0.0;
+          double av = 0.0, bv = 0.0;
           if (xin && ys + i < d.y_max) {
             d.z[c0 + i * d.S] = zl[i];
-            v = rl[i] * zl[i];
+            av = rl[i];
+            bv = zl[i];
           }
-          acc[0] = acc[0] + v;
+          acc[0] = accum<F>(acc[0], av, bv);
         }
       }
     } else {
 #pragma unroll 4
       for (int j = 0; j < TH; j++) {
         const int y = y0 + j;
-        double v = 0.0;
+        double av = 0.0, bv = 0.0;
         if (xin && y < d.y_max) {
           const long long c = cidx(d, x, y);
-          d.u[c] = d.u[c] + alpha * d.p[c];
-          const double rv = d.r[c] - alpha * d.w[c];
-          d.r[c] = rv;
+          const double rv = ur_update<F>(d, c, alpha);
+          av = rv;
           if (d.prec == PREC_JAC_DIAG) {
             const double zv = rv * d.Mi[c];
             d.z[c] = zv;
-            v = rv * zv;
+            bv = zv;
           } else {
-            v = rv * rv;
+            bv = rv;
           }
         }
-        acc[0] = acc[0] + v;
+        acc[0] = accum<F>(acc[0], av, bv);
       }
     }
   });
@@ -468,7 +491,7 @@ __global__ void __launch_bounds__(kBlock)
 // tea_leaf_cg_solve_calc_p, tea_leaf_cg_cl.cl:141-160.  In the
 // device-resident loop it runs once per calc_ur that ran, with that
 // iteration's beta.
-template <int TH>
+template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock)
     k_cg_calc_p(Dev d, Red red, double beta, ResState* st,
                 unsigned int* counter) {
@@ -478,15 +501,13 @@ __global__ void __launch_bounds__(kBlock)
   }
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
+    const double* src = d.prec != PREC_NONE ? d.z : d.r;
 #pragma unroll 4
     for (int j = 0; j < TH; j++) {
       const int y = y0 + j;
       if (y < d.y_max) {
         const long long c = cidx(d, x, y);
-        if (d.prec != PREC_NONE)
-          d.p[c] = d.z[c] + beta * d.p[c];
-        else
-          d.p[c] = d.r[c] + beta * d.p[c];
+        d.p[c] = F ? __fma_rn(beta, d.p[c], src[c]) : src[c] + beta * d.p[c];
       }
     }
   });
@@ -496,11 +517,21 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+// a p + bl br: the Chebyshev / PPCG coefficient update
+// alpha p + beta M^-1 r of tea_leaf_cheby_cl.cl:134-144 and
+// tea_leaf_ppcg_cl.cl:137-152, with bl br = beta z, (beta Mi) r, beta r or
+// (beta r) Mi as each reference expression groups it
+template <bool F>
+__device__ __forceinline__ double cheby_update(double a, double p, double bl,
+                                               double br) {
+  return F ? __fma_rn(a, p, bl * br) : a * p + bl * br;
+}
+
 // The Chebyshev residual step shared by tea_leaf_cheby_solve_init_p and
 // tea_leaf_cheby_solve_calc_p (tea_leaf_cheby_cl.cl:4-64, :78-145):
 // w = A u, r = u0 - w, then p from M^-1 r.  mode 0: p = M^-1 r / theta;
 // mode 1: p = alpha p + beta M^-1 r.
-template <int TH>
+template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock)
     k_cheby_p(Dev d, Red red, int mode, double theta, double alpha,
               double beta) {
@@ -515,14 +546,14 @@ __global__ void __launch_bounds__(kBlock)
         for (int i = 0; i < 4; i++) {
           if (ys + i < d.y_max) {
             const long long c = c0 + i * d.S;
-            const double wv = smvp(d, d.u, c);
+            const double wv = smvp<F>(d, d.u, c);
             d.w[c] = wv;
             const double rv = d.u0[c] - wv;
             d.r[c] = rv;
             rl[i] = rv;
           }
         }
-        strip_solve(d, c0, strip_rows(d, ys), rl, zl);
+        strip_solve<F>(d, c0, strip_rows(d, ys), rl, zl);
 #pragma unroll
         for (int i = 0; i < 4; i++) {
           if (ys + i < d.y_max) {
@@ -530,7 +561,7 @@ __global__ void __launch_bounds__(kBlock)
             if (mode == 0)
               d.p[c] = zl[i] / theta;
             else
-              d.p[c] = alpha * d.p[c] + beta * zl[i];
+              d.p[c] = cheby_update<F>(alpha, d.p[c], beta, zl[i]);
           }
         }
       }
@@ -540,7 +571,7 @@ __global__ void __launch_bounds__(kBlock)
         const int y = y0 + j;
         if (y < d.y_max) {
           const long long c = cidx(d, x, y);
-          const double wv = smvp(d, d.u, c);
+          const double wv = smvp<F>(d, d.u, c);
           d.w[c] = wv;
           const double rv = d.u0[c] - wv;
           d.r[c] = rv;
@@ -551,9 +582,9 @@ __global__ void __launch_bounds__(kBlock)
               d.p[c] = rv / theta;
           } else {
             if (d.prec == PREC_JAC_DIAG)
-              d.p[c] = alpha * d.p[c] + beta * d.Mi[c] * rv;
+              d.p[c] = cheby_update<F>(alpha, d.p[c], beta * d.Mi[c], rv);
             else
-              d.p[c] = alpha * d.p[c] + beta * rv;
+              d.p[c] = cheby_update<F>(alpha, d.p[c], beta, rv);
           }
         }
       }
@@ -562,7 +593,7 @@ __global__ void __launch_bounds__(kBlock)
 }
 
 // tea_leaf_cheby_solve_calc_u, tea_leaf_cheby_cl.cl:66-76
-template <int TH>
+template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock) k_cheby_calc_u(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
@@ -579,8 +610,9 @@ __global__ void __launch_bounds__(kBlock) k_cheby_calc_u(Dev d, Red red) {
 
 // M^-1 r with the PPCG forms: tea_leaf_ppcg_solve_init_sd
 // (tea_leaf_ppcg_cl.cl:4-60, mode 0: sd = M^-1 r / theta) and
-// tea_leaf_ppcg_solve_calc_sd (:90-155, mode 1: sd = alpha sd + beta M^-1 r)
-template <int TH>
+// tea_leaf_ppcg_solve_calc_sd (:90-155, mode 1: sd = alpha sd + beta M^-1 r,
+// diagonal case alpha sd + (beta r) Mi)
+template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock)
     k_ppcg_sd(Dev d, Red red, int mode, double theta, double alpha,
               double beta) {
@@ -594,7 +626,7 @@ __global__ void __launch_bounds__(kBlock)
 #pragma unroll
         for (int i = 0; i < 4; i++)
           rl[i] = (ys + i < d.y_max) ? d.r[c0 + i * d.S] : 0.0;
-        strip_solve(d, c0, strip_rows(d, ys), rl, zl);
+        strip_solve<F>(d, c0, strip_rows(d, ys), rl, zl);
 #pragma unroll
         for (int i = 0; i < 4; i++) {
           if (ys + i < d.y_max) {
@@ -602,7 +634,7 @@ __global__ void __launch_bounds__(kBlock)
             if (mode == 0)
               d.sd[c] = zl[i] / theta;
             else
-              d.sd[c] = alpha * d.sd[c] + beta * zl[i];
+              d.sd[c] = cheby_update<F>(alpha, d.sd[c], beta, zl[i]);
           }
         }
       }
@@ -620,9 +652,9 @@ __global__ void __launch_bounds__(kBlock)
               d.sd[c] = rv / theta;
           } else {
             if (d.prec == PREC_JAC_DIAG)
-              d.sd[c] = alpha * d.sd[c] + beta * rv * d.Mi[c];
+              d.sd[c] = cheby_update<F>(alpha, d.sd[c], beta * rv, d.Mi[c]);
             else
-              d.sd[c] = alpha * d.sd[c] + beta * rv;
+              d.sd[c] = cheby_update<F>(alpha, d.sd[c], beta, rv);
           }
         }
       }
@@ -631,7 +663,7 @@ __global__ void __launch_bounds__(kBlock)
 }
 
 // tea_leaf_ppcg_solve_update_r, tea_leaf_ppcg_cl.cl:62-88
-template <int TH>
+template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock) k_ppcg_update_r(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
@@ -641,7 +673,7 @@ __global__ void __launch_bounds__(kBlock) k_ppcg_update_r(Dev d, Red red) {
       if (y < d.y_max) {
         const long long c = cidx(d, x, y);
         d.u[c] = d.u[c] + d.sd[c];
-        const double result = smvp(d, d.sd, c);
+        const double result = smvp<F>(d, d.sd, c);
         d.r[c] = d.r[c] - result;
       }
     }
@@ -650,7 +682,7 @@ __global__ void __launch_bounds__(kBlock) k_ppcg_update_r(Dev d, Red red) {
 
 // tea_leaf_jacobi_copy_u, tea_leaf_jacobi_cl.cl:3-13 (un is vector_Mi, as
 // in the reference, ocl_kernels.cpp:576-585)
-template <int TH>
+template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock) k_jacobi_copy_u(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
@@ -665,8 +697,9 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_copy_u(Dev d, Red red) {
   });
 }
 
-// tea_leaf_jacobi_solve, tea_leaf_jacobi_cl.cl:15-42
-template <int TH>
+// tea_leaf_jacobi_solve, tea_leaf_jacobi_cl.cl:15-42 (the same arithmetic in
+// both forms; its denominator associates differently from the diagonal)
+template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock) k_jacobi_solve(Dev d, Red red) {
   tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
     const long long S = d.S;
@@ -691,7 +724,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_solve(Dev d, Red red) {
 }
 
 // tea_leaf_finalise, tea_leaf_common_cl.cl:4-15
-template <int TH>
+template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock) k_finalise(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
@@ -707,8 +740,8 @@ __global__ void __launch_bounds__(kBlock) k_finalise(Dev d, Red red) {
 }
 
 // field_summary, field_summary_cl.cl:3-43 (energy argument bound to energy1,
-// ocl_kernels.cpp:466-469)
-template <int TH>
+// ocl_kernels.cpp:466-469); the same arithmetic in both forms
+template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock) k_field_summary(Dev d, Red red) {
   tile_driver<TH, 4>(d, red, [&](int x, int y0, bool xin, double* acc) {
 #pragma unroll 2
@@ -728,6 +761,22 @@ __global__ void __launch_bounds__(kBlock) k_field_summary(Dev d, Red red) {
       acc[1] = acc[1] + v1;
       acc[2] = acc[2] + v2;
       acc[3] = acc[3] + v3;
+    }
+  });
+}
+
+// The diagonal 1 + (Ky_n + Ky_c) + (Kx_e + Kx_c) of every interior cell, in
+// the association of the reference's inline expression
+template <int TH, bool F>
+__global__ void __launch_bounds__(kBlock) k_init_diag(Dev d, Red red) {
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      if (y < d.y_max) {
+        const long long c = cidx(d, x, y);
+        d.diag[c] = (1.0 + (d.Ky[c + d.S] + d.Ky[c]) + (d.Kx[c + 1] + d.Kx[c]));
+      }
     }
   });
 }
@@ -793,6 +842,10 @@ void launch_dot(Chunk& c, const double* a, const double* b) {
   TH_DISPATCH(c, "tea_leaf_calc_2norm", k_dot, c.dev(), c.red(), a, b);
 }
 
+void launch_init_diag(Chunk& c) {
+  TH_DISPATCH(c, "tea_leaf_init_diag", k_init_diag, c.dev(), c.red());
+}
+
 void launch_init_jac_diag(Chunk& c) {
   const Dev d = c.dev();
   launch_2d(c, "tea_leaf_init_jac_diag", d.xs, d.ys, k_init_jac_diag, d);
@@ -800,7 +853,8 @@ void launch_init_jac_diag(Chunk& c) {
 
 void launch_block_init(Chunk& c) {
   const Dev d = c.dev();
-  launch_2d(c, "tea_leaf_block_init", d.x_max, (d.y_max + 3) / 4, k_block_init, d);
+  launch_2d(c, "tea_leaf_block_init", d.x_max, (d.y_max + 3) / 4, k_block_init, d,
+            c.fused ? 1 : 0);
 }
 
 void launch_cg_init_p(Chunk& c) {
@@ -886,19 +940,28 @@ static int tile_grid(Chunk& c, void (*kernel)(KArgs...)) {
   return (int)std::max<long long>(1, std::min<long long>(c.dev().ns, cap));
 }
 
-template <int TH>
-static void enqueue_resident_iterations(Chunk& c, int iters) {
+template <int TH, bool F>
+static void enqueue_resident_iterations_t(Chunk& c, int iters) {
   const Dev d = c.dev();
   const Red red = c.red();
-  const int gw = tile_grid(c, k_cg_calc_w<TH>);
-  const int gu = tile_grid(c, k_cg_calc_ur<TH>);
-  const int gp = tile_grid(c, k_cg_calc_p<TH>);
+  const int gw = tile_grid(c, k_cg_calc_w<TH, F>);
+  const int gu = tile_grid(c, k_cg_calc_ur<TH, F>);
+  const int gp = tile_grid(c, k_cg_calc_p<TH, F>);
   for (int i = 0; i < iters; i++) {
-    k_cg_calc_w<TH><<<gw, kBlock, 0, c.stream>>>(d, red, c.res_state);
-    k_cg_calc_ur<TH><<<gu, kBlock, 0, c.stream>>>(d, red, 0.0, c.res_state);
-    k_cg_calc_p<TH><<<gp, kBlock, 0, c.stream>>>(d, red, 0.0, c.res_state,
-                                                 c.res_counter);
+    k_cg_calc_w<TH, F><<<gw, kBlock, 0, c.stream>>>(d, red, c.res_state);
+    k_cg_calc_ur<TH, F><<<gu, kBlock, 0, c.stream>>>(d, red, 0.0, c.res_state);
+    k_cg_calc_p<TH, F><<<gp, kBlock, 0, c.stream>>>(d, red, 0.0, c.res_state,
+                                                    c.res_counter);
   }
+}
+
+static void enqueue_resident_iterations(Chunk& c, int iters) {
+  if (c.TH == 16)
+    c.fused ? enqueue_resident_iterations_t<16, true>(c, iters)
+            : enqueue_resident_iterations_t<16, false>(c, iters);
+  else
+    c.fused ? enqueue_resident_iterations_t<4, true>(c, iters)
+            : enqueue_resident_iterations_t<4, false>(c, iters);
 }
 
 void resident_release() {
@@ -963,10 +1026,7 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
     if (!check_cuda(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal),
                     "graph capture"))
       return -1;
-    if (c.TH == 16)
-      enqueue_resident_iterations<16>(c, batch);
-    else
-      enqueue_resident_iterations<4>(c, batch);
+    enqueue_resident_iterations(c, batch);
     if (!check_cuda(cudaStreamEndCapture(c.stream, &graph), "graph capture end") ||
         !check_cuda(cudaGraphInstantiate(&c.res_graph, graph, 0), "graph instantiate"))
       return -1;
@@ -985,10 +1045,7 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
       if (!check_cuda(cudaGraphLaunch(c.res_graph, c.stream), "graph launch"))
         return -1;
     } else {
-      if (c.TH == 16)
-        enqueue_resident_iterations<16>(c, batch);
-      else
-        enqueue_resident_iterations<4>(c, batch);
+      enqueue_resident_iterations(c, batch);
       check_cuda(cudaGetLastError(), "resident launch");
     }
     for (int i = 0; i < 3 * batch; i++) count_launch("resident_cg");
@@ -1013,6 +1070,57 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
       return -1;
   }
   return 0;
+}
+
+}  // namespace tea
+
+namespace tea {
+
+// FP64 pipe throughput probe: every thread runs 8 independent fused
+// multiply-add chains, so the FP64 pipe, not latency, sets the time.
+__global__ void k_fp64_rate(double* out, int iters, double b, double c) {
+  double a0 = threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4,
+         a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+  for (int i = 0; i < iters; i++) {
+    a0 = __fma_rn(a0, b, c);
+    a1 = __fma_rn(a1, b, c);
+    a2 = __fma_rn(a2, b, c);
+    a3 = __fma_rn(a3, b, c);
+    a4 = __fma_rn(a4, b, c);
+    a5 = __fma_rn(a5, b, c);
+    a6 = __fma_rn(a6, b, c);
+    a7 = __fma_rn(a7, b, c);
+  }
+  const double s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+  if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+
+double measure_fp64_rate() {
+  Chunk& c = chunk();
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  double* out = nullptr;
+  if (!check_cuda(cudaMalloc(&out, sizeof(double)), "probe alloc")) return -1.0;
+  cudaStream_t s = c.stream;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  k_fp64_rate<<<blocks, threads, 0, s>>>(out, 64, 0.999, 1e-3);  // warm-up
+  cudaEventRecord(e0, s);
+  k_fp64_rate<<<blocks, threads, 0, s>>>(out, iters, 0.999, 1e-3);
+  cudaEventRecord(e1, s);
+  cudaEventSynchronize(e1);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  count_launch("fp64_rate");
+  count_launch("fp64_rate");
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  const double instr = (double)blocks * threads * iters * 8.0;
+  return instr / (ms * 1e-3);
 }
 
 }  // namespace tea

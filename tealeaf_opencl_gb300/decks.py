@@ -45,3 +45,43 @@ def five_state_deck(cells, solver="cg", prec="none", steps=10, eps=1e-15,
         lines.append(extra.rstrip("\n"))
     lines.append("*endtea")
     return "\n".join(lines) + "\n"
+
+
+FIVE_STATE_TABLE = dict(density=[100.0, 0.1, 0.1, 0.1, 0.1],
+                        energy=[1e-4, 25.0, 0.1, 0.1, 0.1],
+                        xmin=[0.0, 0.0, 1.0, 5.0, 5.0], xmax=[0.0, 1.0, 6.0, 6.0, 10.0],
+                        ymin=[0.0, 1.0, 1.0, 1.0, 7.0], ymax=[0.0, 2.0, 2.0, 8.0, 8.0],
+                        radius=[0.0] * 5, geometry=[0, 1, 1, 1, 1])
+
+
+def setup_five_state(chunk, x_cells, y_cells=None, width=10.0):
+    """Set up the five-state problem on a chunk through the C-ABI entry
+    points, as start.f90 does: mesh, states (boxes shrunk by a hundredth of
+    a cell, read_input.f90:314-327), energy1 = energy0."""
+    y_cells = x_cells if y_cells is None else y_cells
+    dx, dy = width / x_cells, width / y_cells
+    s = {k: list(v) for k, v in FIVE_STATE_TABLE.items()}
+    for n in range(1, 5):
+        s["xmin"][n] += dx / 100.0
+        s["ymin"][n] += dy / 100.0
+        s["xmax"][n] -= dx / 100.0
+        s["ymax"][n] -= dy / 100.0
+    chunk.initialise_chunk(0.0, 0.0, dx, dy)
+    chunk.generate_chunk(s["density"], s["energy"], s["xmin"], s["xmax"], s["ymin"],
+                         s["ymax"], s["radius"], s["geometry"])
+    chunk.set_field()
+
+
+def chebyshev_coefficients(eigmin, eigmax, n):
+    """tea_calc_ch_coefs (tea_leaf_cheby.f90:145-172)."""
+    theta = (eigmax + eigmin) / 2
+    delta = (eigmax - eigmin) / 2
+    sigma = theta / delta
+    rho_old = 1.0 / sigma
+    alphas, betas = [], []
+    for _ in range(n):
+        rho_new = 1.0 / (2.0 * sigma - rho_old)
+        alphas.append(rho_new * rho_old)
+        betas.append(2.0 * rho_new / delta)
+        rho_old = rho_new
+    return alphas, betas, theta

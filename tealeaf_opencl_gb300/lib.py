@@ -33,13 +33,15 @@ REFERENCE_SYMBOLS = [
     "print_opencl_profiling_info_", "ocl_pack_buffers_", "ocl_unpack_buffers_",
 ]
 EXTRA_SYMBOLS = [
-    "tea_gb300_configure", "tea_gb300_set_abort_on_error", "tea_gb300_last_error",
+    "tea_gb300_configure", "tea_gb300_set_arithmetic", "tea_gb300_get_arithmetic",
+    "tea_gb300_set_abort_on_error", "tea_gb300_last_error",
     "tea_gb300_finalise", "tea_gb300_read_field", "tea_gb300_write_field",
     "tea_gb300_read_field_padded", "tea_gb300_write_field_padded",
     "tea_gb300_reduction_rows", "tea_gb300_kernel_launches", "tea_gb300_stream",
     "tea_gb300_chunk_info", "tea_gb300_event_record", "tea_gb300_event_elapsed_ms",
     "tea_gb300_synchronize", "tea_gb300_host_alloc", "tea_gb300_host_free",
     "tea_gb300_kernel_timer_select", "tea_gb300_kernel_timer_read",
+    "tea_gb300_kernel_timer_read_name", "tea_gb300_fp64_rate",
     "tea_gb300_driver_open", "tea_gb300_driver_step", "tea_gb300_driver_close",
 ]
 
@@ -107,6 +109,8 @@ def load(build=True):
         "ocl_unpack_buffers_": (v, [PI, PI, PI, PI, PD]),
         "tea_gb300_configure": (i, [i, i, i, i]),
         "tea_gb300_set_abort_on_error": (v, [i]),
+        "tea_gb300_set_arithmetic": (i, [i]),
+        "tea_gb300_get_arithmetic": (i, []),
         "tea_gb300_last_error": (i, [C.c_char_p, i]),
         "tea_gb300_finalise": (v, []),
         "tea_gb300_read_field": (i, [i, PD]),
@@ -124,6 +128,8 @@ def load(build=True):
         "tea_gb300_host_free": (v, [C.c_void_p]),
         "tea_gb300_kernel_timer_select": (i, [C.c_char_p]),
         "tea_gb300_kernel_timer_read": (i, [PD, C.POINTER(C.c_longlong)]),
+        "tea_gb300_kernel_timer_read_name": (i, [C.c_char_p, PD, C.POINTER(C.c_longlong)]),
+        "tea_gb300_fp64_rate": (d, []),
         "tea_gb300_driver_open": (i, [C.c_char_p, C.c_char_p, i, i]),
         "tea_gb300_driver_step": (i, [C.POINTER(StepInfo)]),
         "tea_gb300_driver_close": (v, []),
@@ -174,6 +180,9 @@ class Chunk:
         check()
         self.x_max, self.y_max, self.halo = x_max, y_max, halo
         self.neighbours = np.full(4, EXTERNAL_FACE, dtype=np.int32)
+
+    def set_arithmetic(self, fused):
+        load().tea_gb300_set_arithmetic(1 if fused else 0)
 
     # -- setup -------------------------------------------------------------
     def initialise_chunk(self, xmin, ymin, dx, dy):

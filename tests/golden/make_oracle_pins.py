@@ -4,7 +4,9 @@ tests/test_gpu_runs.py compares the GPU runs of test problems 2 and 3
 (960^2 and 3840^2 CG, tens of thousands of iterations) with these records
 bit for bit: per-step iteration counts and the final temperature (as a hex
 float).  The oracle takes minutes to hours on a CPU for these, so the
-results are kept as a fixture.  Usage: make_oracle_pins.py TP [TP ...]
+results are kept as a fixture: oracle_pins.json for the exact arithmetic
+form, oracle_pins_fused.json for the fused one.
+Usage: make_oracle_pins.py [--fused] TP [TP ...]
 """
 import json
 import os
@@ -17,17 +19,20 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from oracle import oracle  # noqa: E402
 
 
-def main(tps):
-    path = os.path.join(HERE, "oracle_pins.json")
+def main(tps, fused):
+    path = os.path.join(HERE, "oracle_pins_fused.json" if fused else "oracle_pins.json")
     pins = json.load(open(path)) if os.path.exists(path) else {}
     meta = json.load(open(os.path.join(HERE, "test_problems.json")))
     for tp in tps:
         p = meta["problems"][str(tp)]
         deck = open(os.path.join(HERE, p["deck"])).read()
+        deck = deck.replace("*endtea", "tl_arithmetic %s\n*endtea"
+                            % ("fused" if fused else "exact"), 1)
         t0 = time.time()
         res = oracle.run_deck(deck)
         pins[str(tp)] = {
             "deck": p["deck"],
+            "arithmetic": "fused" if fused else "exact",
             "temp": res.final_temp,
             "temp_hex": float(res.final_temp).hex(),
             "golden_temp": p["temp"],
@@ -41,4 +46,6 @@ def main(tps):
 
 
 if __name__ == "__main__":
-    main([int(a) for a in sys.argv[1:]] or [2])
+    args = sys.argv[1:]
+    fused = "--fused" in args
+    main([int(a) for a in args if a != "--fused"] or [2], fused)

@@ -64,8 +64,9 @@ def ch_coefs(eigmin, eigmax, n):
 
 def run(ch, x, y, solver, prec, halo=1, reflective=False, coef=1, cg_iters=6,
         cheby_iters=4, inner=5, jacobi_iters=4, dt=0.004, lognormal_seed=None,
-        states=FIVE, snapshots=True):
+        states=FIVE, snapshots=True, fused=True):
     rec = []
+    ch.set_arithmetic(fused)
 
     def snap(tag):
         if snapshots:

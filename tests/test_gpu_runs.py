@@ -24,9 +24,14 @@ def problem(tp):
     return open(os.path.join(GOLD, p["deck"])).read(), p["temp"]
 
 
-def pins():
-    path = os.path.join(GOLD, "oracle_pins.json")
+def pins(mode):
+    name = "oracle_pins_fused.json" if mode == "fused" else "oracle_pins.json"
+    path = os.path.join(GOLD, name)
     return json.load(open(path)) if os.path.exists(path) else {}
+
+
+def with_arithmetic(deck, mode):
+    return deck.replace("*endtea", "tl_arithmetic %s\n*endtea" % mode, 1)
 
 
 def gpu_run(deck, mode=lib.DRIVER_PER_CALL):
@@ -44,23 +49,27 @@ def assert_matches_oracle(steps, res):
     assert (last.vol, last.mass, last.ie, last.temp) == tuple(final[[1, 2, 4, 5]])
 
 
+@pytest.mark.parametrize("mode", ["exact", "fused"])
 @pytest.mark.parametrize("tp", [1, 6])
-def test_test_problem_matches_golden_and_oracle(tp):
+def test_test_problem_matches_golden_and_oracle(tp, mode):
     deck, temp = problem(tp)
+    deck = with_arithmetic(deck, mode)
     steps = gpu_run(deck)
     assert steps[-1].qa_passed == 1, steps[-1].qa_diff
     assert abs(100.0 * steps[-1].temp / temp - 100.0) < 0.001
     assert_matches_oracle(steps, oracle.run_deck(deck))
 
 
+@pytest.mark.parametrize("mode", ["exact", "fused"])
 @pytest.mark.parametrize("tp", [2, 3])
-def test_cg_test_problem_matches_golden_and_oracle_pin(tp):
+def test_cg_test_problem_matches_golden_and_oracle_pin(tp, mode):
     deck, temp = problem(tp)
-    steps = gpu_run(deck, mode=lib.DRIVER_RESIDENT)
+    steps = gpu_run(with_arithmetic(deck, mode), mode=lib.DRIVER_RESIDENT)
     assert steps[-1].qa_passed == 1, steps[-1].qa_diff
-    pin = pins().get(str(tp))
+    pin = pins(mode).get(str(tp))
     if pin is None:
-        pytest.skip("no oracle pin recorded for test problem %d" % tp)
+        pytest.skip("no oracle pin recorded for test problem %d (%s)" % (tp, mode))
+    assert pin["arithmetic"] == mode if "arithmetic" in pin else mode == "exact"
     assert [s.iterations for s in steps] == pin["iterations"]
     assert steps[-1].temp == float.fromhex(pin["temp_hex"])
 
@@ -72,10 +81,12 @@ def test_long_cg_test_problems_match_golden(tp):
     assert steps[-1].qa_passed == 1, steps[-1].qa_diff
 
 
-def test_c1_512_cg_jac_diag_matches_oracle():
+@pytest.mark.parametrize("mode", ["exact", "fused"])
+def test_c1_512_cg_jac_diag_matches_oracle(mode):
     """512x512 CG + diagonal Jacobi, eps 1e-15, 10 steps."""
     deck = decks.five_state_deck(512, solver="cg", prec="jac_diag", steps=10,
-                                 eps=1e-15, max_iters=5000)
+                                 eps=1e-15, max_iters=5000,
+                                 extra="tl_arithmetic %s" % mode)
     res = oracle.run_deck(deck)
     per_call = gpu_run(deck)
     assert_matches_oracle(per_call, res)

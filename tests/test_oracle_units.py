@@ -56,6 +56,14 @@ def test_reduce_order_matches_python_restatement(shape):
     assert oracle.reduce(a) == py_reduce(a)
 
 
+def test_reduce_pairs_unfused_is_reduce_of_products():
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal((37, 61))
+    b = rng.standard_normal((37, 61))
+    assert oracle.reduce_pairs(a, b, 0) == oracle.reduce(a * b)
+    assert abs(oracle.reduce_pairs(a, b, 1) - oracle.reduce(a * b)) < 1e-12
+
+
 def test_reduce_exact_on_integers():
     a = np.arange(64 * 300, dtype=np.float64).reshape(64, 300)
     assert oracle.reduce(a) == a.sum()
@@ -94,6 +102,7 @@ def test_update_halo_matches_four_pass_reflection(H, d):
 def test_block_jacobi_solves_each_strip(x, y, H):
     """z = M^-1 r with M the 4-row tridiagonal strips of the operator."""
     ch = oracle.Chunk(x, y, H, 2, 3)
+    ch.set_arithmetic(True)
     scenarios.setup(ch, x, y, lognormal_seed=3)
     ch.common_init(1, 0.004)
     rng = np.random.default_rng(1)
