@@ -258,6 +258,28 @@ int tea_gb300_kernel_timer_read_name(const char* name, double* total_ms,
  * current GPU (independent chains, all SMs).  Needs an initialised chunk. */
 double tea_gb300_fp64_rate(void);
 
+/* No counterpart in the reference.  The dot product sum(a*b) over the
+ * interior of two padded FP64 fields, for callers that cannot allocate GPU
+ * memory (their device memory is held by another allocator, or they must
+ * not call cudaMalloc on this path).  The caller passes device pointers to
+ * the inputs and to one double for the result; nothing is allocated.  The
+ * reduction's scratch is a fixed device array inside this library (512 KiB,
+ * held on every GPU that loads the library until the process exits), which
+ * limits the interior to at most 65536 partial sums (16384 x 16384 cells);
+ * larger sizes are rejected with an error.  Layout: element (col,row) at
+ * a[row*stride + col], interior at [halo, halo+x_max) x [halo, halo+y_max).
+ * Summation order and arithmetic form are those of
+ * tea_leaf_calc_2norm_kernel_ocl_, so equal inputs give equal bits.
+ * Queued on `stream` (a cudaStream_t; NULL for the default stream) and
+ * returns before the GPU finishes.  The first call on a device looks up
+ * the scratch's device address; make that first call before any stream
+ * capture.  All calls share the scratch: calls that can overlap on the GPU
+ * (different streams, no ordering between them) race and give wrong
+ * results.  Returns 0, or -1 (see tea_gb300_last_error). */
+int tea_gb300_dot_noalloc(const double* a, const double* b, int x_max,
+                          int y_max, int halo, long long stride,
+                          double* result, void* stream);
+
 /* Waits for all work queued on the library's stream. */
 int tea_gb300_synchronize(void);
 

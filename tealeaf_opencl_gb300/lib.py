@@ -42,6 +42,7 @@ EXTRA_SYMBOLS = [
     "tea_gb300_synchronize", "tea_gb300_host_alloc", "tea_gb300_host_free",
     "tea_gb300_kernel_timer_select", "tea_gb300_kernel_timer_read",
     "tea_gb300_kernel_timer_read_name", "tea_gb300_fp64_rate",
+    "tea_gb300_dot_noalloc",
     "tea_gb300_driver_open", "tea_gb300_driver_step", "tea_gb300_driver_close",
 ]
 
@@ -130,6 +131,8 @@ def load(build=True):
         "tea_gb300_kernel_timer_read": (i, [PD, C.POINTER(C.c_longlong)]),
         "tea_gb300_kernel_timer_read_name": (i, [C.c_char_p, PD, C.POINTER(C.c_longlong)]),
         "tea_gb300_fp64_rate": (d, []),
+        "tea_gb300_dot_noalloc": (i, [C.c_void_p, C.c_void_p, i, i, i, C.c_longlong,
+                                      C.c_void_p, C.c_void_p]),
         "tea_gb300_driver_open": (i, [C.c_char_p, C.c_char_p, i, i]),
         "tea_gb300_driver_step": (i, [C.POINTER(StepInfo)]),
         "tea_gb300_driver_close": (v, []),
