@@ -387,6 +387,62 @@ def run_kernels(args):
     return out
 
 
+def lognormal_factor(n, sigma=0.5, corr=8.0, seed=2024):
+    """exp(sigma g) for a unit-variance Gaussian field g with correlation
+    exp(-d^2 / (2 corr^2)): seeded white noise filtered by a Gaussian of
+    width corr/sqrt(2) (spectrally), then renormalised."""
+    import numpy as np
+    rng = np.random.Generator(np.random.Philox(seed))
+    w = rng.standard_normal((n, n))
+    k = np.fft.fftfreq(n)
+    s = corr / np.sqrt(2.0)
+    gk = np.exp(-2.0 * (np.pi * s) ** 2 * (k[:, None] ** 2 + k[None, :] ** 2))
+    g = np.fft.ifft2(np.fft.fft2(w) * gk).real
+    g = (g - g.mean()) / g.std()
+    return np.exp(sigma * g)
+
+
+def run_mixed(args):
+    """FP64 CG and FP32-inner/FP64-refined CG to the same true relative
+    FP64 residual (1e-10), on the same problem; wall time per timestep."""
+    from tealeaf_opencl_gb300 import decks, lib
+    L = lib.load()
+    cells = args.cells
+    factor = lognormal_factor(cells) if args.lognormal else None
+    out = {"mode": "mixed", "cells": cells * cells, "steps": args.steps,
+           "lognormal": bool(args.lognormal), "tol": 1e-10}
+    ncell = cells * cells
+    for name, extra, mode in (("fp64", "tl_exit_true_residual", lib.DRIVER_RESIDENT),
+                              ("mixed", "tl_mixed_precision\ntl_mixed_inner_eps 1e-5",
+                               lib.DRIVER_PER_CALL)):
+        deck = decks.five_state_deck(cells, solver="cg", prec="jac_diag",
+                                     steps=args.steps, eps=1e-10, max_iters=100000,
+                                     summary_frequency=0, check_result=True, extra=extra)
+        drv = lib.Driver(deck, mode=mode)
+        if factor is not None:
+            lib.write_field("density", lib.read_field("density") * factor)
+        L.tea_gb300_synchronize()
+        times, infos = [], []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            infos.append(drv.step())
+            L.tea_gb300_synchronize()
+            times.append(time.perf_counter() - t0)
+        drv.close()
+        last = infos[-1]
+        out[name] = {"seconds": sum(times), "step_seconds": times,
+                     "iterations": [i.iterations for i in infos],
+                     "corrections": [i.outer_corrections for i in infos],
+                     "relative_residual": [i.relative_residual if name == "mixed"
+                                           else i.exact_error for i in infos],
+                     "field_summary": {"vol": last.vol, "mass": last.mass,
+                                       "ie": last.ie, "temp": last.temp}}
+    a, b = out["fp64"]["field_summary"], out["mixed"]["field_summary"]
+    out["field_summary_rel_diff"] = {k: abs(a[k] - b[k]) / abs(a[k]) for k in a}
+    out["time_ratio_mixed_over_fp64"] = out["mixed"]["seconds"] / out["fp64"]["seconds"]
+    return out
+
+
 def cpu_sample(name, steps_timed, cap):
     """Oracle on the same deck: one warm-up step, then steps_timed steps,
     every step capped at `cap` outer iterations; returns (value, detail)."""
@@ -447,8 +503,12 @@ def main():
     ap.add_argument("--cap", type=int, default=0,
                     help="limit solver iterations per GPU step (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="run", choices=["run", "kernels"],
-                    help="kernels: time each hot entry point on the workload's grid")
+    ap.add_argument("--mode", default="run", choices=["run", "kernels", "mixed"],
+                    help="kernels: time each hot entry point on the workload's grid; "
+                         "mixed: FP64 vs FP32-inner/FP64-refined CG to 1e-10")
+    ap.add_argument("--cells", type=int, default=4096, help="grid side for --mode mixed")
+    ap.add_argument("--lognormal", action="store_true",
+                    help="--mode mixed: density times a seeded log-normal field")
     ap.add_argument("--reps", type=int, default=20)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -467,6 +527,9 @@ def main():
 
     if args.mode == "kernels":
         print(json.dumps(run_kernels(args)))
+        return
+    if args.mode == "mixed":
+        print(json.dumps(run_mixed(args)))
         return
 
     dist = Dist()

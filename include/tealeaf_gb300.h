@@ -280,6 +280,26 @@ int tea_gb300_dot_noalloc(const double* a, const double* b, int x_max,
                           int y_max, int halo, long long stride,
                           double* result, void* stream);
 
+/* No counterpart in the reference.  Mixed-precision solve of the current
+ * timestep's system (I + L_K) u = u0 on the chunk, after
+ * tea_leaf_common_init_kernel_ocl_: FP32 diagonally preconditioned CG inner
+ * solves inside an FP64 defect-correction loop.  The FP64 steps are the
+ * residual u0 - A u, the accumulation u += d and every dot product; the
+ * FP32 ones are the inner vectors and the operator copies.  Stops when
+ * ||u0 - A u||_2 <= tol * (its value at entry), or after max_outer
+ * corrections; each inner solve stops when its preconditioned residual has
+ * fallen by inner_tol or after max_inner iterations.  u holds the FP64
+ * solution on return.  Returns 0 or -1. */
+typedef struct {
+  int outer_iterations;          /* FP64 corrections made */
+  long long inner_iterations;    /* FP32 CG iterations, all corrections */
+  double initial_residual;       /* ||u0 - A u||_2 at entry */
+  double final_residual;         /* ||u0 - A u||_2 at return, FP64 */
+  double relative_residual;      /* their ratio */
+} tea_gb300_mixed_info;
+int tea_gb300_mixed_solve(double tol, double inner_tol, int max_outer,
+                          int max_inner, tea_gb300_mixed_info* info);
+
 /* Waits for all work queued on the library's stream. */
 int tea_gb300_synchronize(void);
 
@@ -306,6 +326,8 @@ typedef struct {
   int complete;           /* 1 after the last step of the deck */
   int qa_passed;          /* test problem check: 1, 0, or -1 (none) */
   double qa_diff;
+  int outer_corrections;  /* mixed precision: FP64 corrections (else 0) */
+  double relative_residual; /* mixed precision: final ||r||/||r0|| (FP64) */
 } tea_gb300_step_info;
 
 /* Parses a tea.in deck (its text), sets up the problem on the GPU (as

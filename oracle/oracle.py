@@ -35,6 +35,8 @@ class OracleResult(C.Structure):
         ("total_inner_iterations", C.c_longlong),
         ("qa_passed", C.c_int),
         ("qa_diff", C.c_double),
+        ("outer_corrections", C.c_int * 1024),
+        ("relative_residual", C.c_double * 1024),
     ]
 
     def summaries(self):
@@ -42,6 +44,14 @@ class OracleResult(C.Structure):
         start = self.n_summaries - n
         rows = [list(self.summary[(start + i) % 64]) for i in range(n)]
         return np.array(rows)
+
+
+class MixedInfo(C.Structure):
+    _fields_ = [
+        ("outer_iterations", C.c_int), ("inner_iterations", C.c_longlong),
+        ("initial_residual", C.c_double), ("final_residual", C.c_double),
+        ("relative_residual", C.c_double),
+    ]
 
 
 _lib = None
@@ -87,6 +97,7 @@ def lib():
             "oracle_run_deck": (i, [C.c_char_p, C.c_char_p, i,
                                     C.POINTER(OracleResult), C.c_char_p, i]),
             "oracle_num_threads": (i, []),
+            "oracle_mixed_solve": (i, [d, d, i, i, C.POINTER(MixedInfo)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -208,6 +219,12 @@ class Chunk:
         out = [C.c_double() for _ in range(4)]
         lib().oracle_field_summary(*[C.byref(o) for o in out])
         return tuple(o.value for o in out)
+
+    def mixed_solve(self, tol, inner_tol=1e-4, max_outer=50, max_inner=10000):
+        info = MixedInfo()
+        if lib().oracle_mixed_solve(tol, inner_tol, max_outer, max_inner, C.byref(info)) != 0:
+            raise RuntimeError("oracle mixed solve failed")
+        return info
 
     def update_halo(self, fields, depth):
         f = np.ascontiguousarray(fields, dtype=np.int32)

@@ -118,6 +118,17 @@ void oracle_set_arithmetic(int fused);
 int oracle_get_arithmetic(void);
 int oracle_reduction_rows(int x_max, int y_max);
 
+/* ---- mixed precision (restates tea_gb300_mixed_solve) ---- */
+typedef struct {
+  int outer_iterations;
+  long long inner_iterations;
+  double initial_residual;
+  double final_residual;
+  double relative_residual;
+} oracle_mixed_info;
+int oracle_mixed_solve(double tol, double inner_tol, int max_outer,
+                       int max_inner, oracle_mixed_info* info);
+
 /* ---- whole runs (restatement of the Fortran driver) ---- */
 typedef struct {
   int n_summaries;      /* field_summary calls made */
@@ -134,6 +145,8 @@ typedef struct {
   long long total_inner_iterations;
   int qa_passed;          /* 1 pass, 0 fail, -1 not a test problem */
   double qa_diff;
+  int outer_corrections[1024]; /* mixed precision: FP64 corrections */
+  double relative_residual[1024];
 } oracle_result;
 
 /* Parse tea.in text and run it.  log_path may be NULL; otherwise a tea.out

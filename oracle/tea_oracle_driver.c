@@ -46,6 +46,9 @@ typedef struct {
   int test_problem;
   int verbose;
   int fused; /* tl_arithmetic: 0 exact, 1 fused (default) */
+  int mixed; /* tl_mixed_precision */
+  double mixed_inner_eps;
+  int mixed_max_outer;
   int number_of_states;
   double s_density[MAX_STATES], s_energy[MAX_STATES];
   double s_xmin[MAX_STATES], s_xmax[MAX_STATES], s_ymin[MAX_STATES],
@@ -184,6 +187,9 @@ static int parse_deck(const char* text, Deck* D, char* err, int errlen) {
   D->solver = ORC_SOLVER_JACOBI;
   D->halo_depth = 1;
   D->fused = 1;
+  D->mixed = 0;
+  D->mixed_inner_eps = 1e-4;
+  D->mixed_max_outer = 50;
 
   Lines L = deck_lines(text);
   int state_max = 0, ok = 1;
@@ -252,6 +258,9 @@ static int parse_deck(const char* text, Deck* D, char* err, int errlen) {
         }
       }
       else if (!strcmp(w, "verbose_on")) D->verbose = 1;
+      else if (!strcmp(w, "tl_mixed_precision")) D->mixed = 1;
+      else if (!strcmp(w, "tl_mixed_inner_eps")) RVAL(D->mixed_inner_eps);
+      else if (!strcmp(w, "tl_mixed_max_outer")) IVAL(D->mixed_max_outer);
       else if (!strcmp(w, "tl_arithmetic")) {
         /* not a reference key: which arithmetic form to use */
         const char* v = next_word(&W);
@@ -561,6 +570,30 @@ static int tea_leaf(Run* R, int step_index) {
   oracle_calc_2norm(1, &initial_residual);
   old_error = initial_residual;
   initial_residual = sqrt(initial_residual);
+
+  if (D->mixed) {
+    oracle_mixed_info mi;
+    oracle_mixed_solve(D->eps, D->mixed_inner_eps, D->mixed_max_outer,
+                       D->max_iters, &mi);
+    logf_(R, "Mixed precision: %d FP64 corrections, %lld FP32 CG iterations, "
+             "relative FP64 residual %14.7E\n",
+          mi.outer_iterations, mi.inner_iterations, mi.relative_residual);
+    oracle_finalise_kernel();
+    int fe[7] = {0, 0, 1, 0, 0, 0, 0};
+    update_halo(R, fe, 1);
+    oracle_result* res = R->R;
+    if (step_index < 1024) {
+      res->iterations[step_index] = (int)mi.inner_iterations;
+      res->inner_iterations[step_index] = 0;
+      res->outer_corrections[step_index] = mi.outer_iterations;
+      res->relative_residual[step_index] = mi.relative_residual;
+      res->conduction_error[step_index] = mi.final_residual / initial_residual;
+      res->exact_error[step_index] = NAN;
+    }
+    res->total_outer_iterations += mi.inner_iterations;
+    free(cg_alphas); free(cg_betas); free(ch_alphas); free(ch_betas);
+    return 0;
+  }
 
   if (use_cg || use_cheby || use_ppcg) oracle_cg_init(&rro);
 

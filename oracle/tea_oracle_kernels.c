@@ -189,8 +189,11 @@ static double* zalloc(long n) {
   return p;
 }
 
+static void mix_free(void);
+
 void oracle_finalise(void) {
   if (!C_ready) return;
+  mix_free();
   double** all[] = {&C.density, &C.energy0, &C.energy1, &C.volume, &C.cellx,
                     &C.celldx,  &C.vertexx, &C.vertexdx, &C.celly, &C.celldy,
                     &C.vertexy, &C.vertexdy, &C.p, &C.r, &C.w, &C.Mi, &C.Kx,
@@ -939,4 +942,165 @@ int oracle_num_threads(void) {
 #else
   return 1;
 #endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* Mixed precision: FP32 inner CG in FP64 defect correction                 */
+/* ------------------------------------------------------------------------ */
+/*
+ * Restates tea_gb300_mixed_solve of the CUDA library (the oracle has no
+ * reference counterpart for it: it is an addition to the reference's
+ * solvers).  FP32 parts use float with fmaf where the CUDA code uses
+ * __fmaf_rn; FP64 parts use the fused form; every sum is reduce_pairs with
+ * fma accumulation.
+ */
+typedef struct {
+  float *Kx, *Ky, *D, *Mi, *d, *r, *p, *w;
+} OrcMix;
+static OrcMix M;
+static long M_n = 0;
+
+static void mix_free(void) {
+  float** f[8] = {&M.Kx, &M.Ky, &M.D, &M.Mi, &M.d, &M.r, &M.p, &M.w};
+  for (int i = 0; i < 8; i++) {
+    free(*f[i]);
+    *f[i] = NULL;
+  }
+  M_n = 0;
+}
+
+static int mix_alloc(void) {
+  if (M_n == C.n2 && M.Kx) return 0;
+  mix_free();
+  float** f[8] = {&M.Kx, &M.Ky, &M.D, &M.Mi, &M.d, &M.r, &M.p, &M.w};
+  for (int i = 0; i < 8; i++) {
+    *f[i] = (float*)calloc((size_t)C.n2, sizeof(float));
+    if (!*f[i]) return -1;
+  }
+  M_n = C.n2;
+  return 0;
+}
+
+static inline double smvp64_fused(const double* x, long c) {
+  const long xs = C.xs;
+  const double D = (1.0 + (C.Ky[c + xs] + C.Ky[c]) + (C.Kx[c + 1] + C.Kx[c]));
+  const double t1 = fma(C.Ky[c], x[c - xs], C.Ky[c + xs] * x[c + xs]);
+  const double t2 = fma(C.Kx[c], x[c - 1], C.Kx[c + 1] * x[c + 1]);
+  return fma(D, x[c], -t1) - t2;
+}
+
+static inline float smvp32(const float* x, long c) {
+  const long xs = C.xs;
+  const float kyn = M.Ky[c + xs], kyc = M.Ky[c];
+  const float kxe = M.Kx[c + 1], kxc = M.Kx[c];
+  const float t1 = fmaf(kyc, x[c - xs], kyn * x[c + xs]);
+  const float t2 = fmaf(kxc, x[c - 1], kxe * x[c + 1]);
+  return fmaf(M.D[c], x[c], -t1) - t2;
+}
+
+/* r64 = u0 - A u; r32 = (float)r64; z = Mi r32; p = z; d = 0.
+ * out[0] = r64.r64, out[1] = r32.z */
+static void mix_residual(double* out) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      const double r64 = C.u0[c] - smvp64_fused(C.u, c);
+      C.r[c] = r64;
+      const float r32 = (float)r64;
+      const float z = M.Mi[c] * r32;
+      M.r[c] = r32;
+      M.p[c] = z;
+      M.d[c] = 0.0f;
+      DOT(0, col, row, r64, r64);
+      DOT(1, col, row, (double)r32, (double)z);
+    }
+  out[0] = reduce_pairs(C.scratch[0], C.scratchb[0], C.x_max, C.y_max, 1);
+  out[1] = reduce_pairs(C.scratch[1], C.scratchb[1], C.x_max, C.y_max, 1);
+}
+
+int oracle_mixed_solve(double tol, double inner_tol, int max_outer,
+                       int max_inner, oracle_mixed_info* info) {
+  const int H = C.H;
+  memset(info, 0, sizeof(*info));
+  if (!C_ready || mix_alloc() != 0) return -1;
+  /* FP32 copies of the operator */
+  for (long i = 0; i < C.n2; i++) {
+    M.Kx[i] = (float)C.Kx[i];
+    M.Ky[i] = (float)C.Ky[i];
+  }
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      const double D =
+          (1.0 + (C.Ky[c + C.xs] + C.Ky[c]) + (C.Kx[c + 1] + C.Kx[c]));
+      M.D[c] = (float)D;
+      M.Mi[c] = (float)(1.0 / D);
+    }
+  double res[2];
+  mix_residual(res);
+  const double rr_first = res[0];
+  info->initial_residual = sqrt(rr_first);
+  int outer = 0;
+  long long inner_total = 0;
+  while (!(sqrt(res[0]) <= tol * sqrt(rr_first)) && outer < max_outer) {
+    double rro = res[1];
+    const double need = 0.25 * tol * sqrt(rr_first) / sqrt(res[0]);
+    const double itol = need > inner_tol ? (need < 0.5 ? need : 0.5) : inner_tol;
+    const double eps2 = itol * itol * res[1];
+    int n = 1, done = 0;
+    for (;;) {
+      /* w = A p, p.w */
+#pragma omp parallel for schedule(static)
+      for (int row = H; row < H + C.y_max; row++)
+        for (int col = H; col < H + C.x_max; col++) {
+          const long c = IDX(col, row);
+          const float wv = smvp32(M.p, c);
+          M.w[c] = wv;
+          DOT(0, col, row, (double)M.p[c], (double)wv);
+        }
+      const double pw = reduce_pairs(C.scratch[0], C.scratchb[0], C.x_max, C.y_max, 1);
+      const double alpha = rro / pw;
+      const float af = (float)alpha;
+#pragma omp parallel for schedule(static)
+      for (int row = H; row < H + C.y_max; row++)
+        for (int col = H; col < H + C.x_max; col++) {
+          const long c = IDX(col, row);
+          M.d[c] = fmaf(af, M.p[c], M.d[c]);
+          const float rv = fmaf(-af, M.w[c], M.r[c]);
+          M.r[c] = rv;
+          const float zv = M.Mi[c] * rv;
+          DOT(0, col, row, (double)rv, (double)zv);
+        }
+      const double rrn = reduce_pairs(C.scratch[0], C.scratchb[0], C.x_max, C.y_max, 1);
+      const double beta = rrn / rro;
+      rro = rrn;
+      done = n;
+      const int stop = (rrn <= eps2 || n >= max_inner);
+      const float bf = (float)beta;
+#pragma omp parallel for schedule(static)
+      for (int row = H; row < H + C.y_max; row++)
+        for (int col = H; col < H + C.x_max; col++) {
+          const long c = IDX(col, row);
+          M.p[c] = fmaf(bf, M.p[c], M.Mi[c] * M.r[c]);
+        }
+      if (stop) break;
+      n++;
+    }
+    inner_total += done;
+#pragma omp parallel for schedule(static)
+    for (int row = H; row < H + C.y_max; row++)
+      for (int col = H; col < H + C.x_max; col++) {
+        const long c = IDX(col, row);
+        C.u[c] = C.u[c] + (double)M.d[c];
+      }
+    outer++;
+    mix_residual(res);
+  }
+  info->outer_iterations = outer;
+  info->inner_iterations = inner_total;
+  info->final_residual = sqrt(res[0]);
+  info->relative_residual = sqrt(res[0]) / sqrt(rr_first);
+  return 0;
 }

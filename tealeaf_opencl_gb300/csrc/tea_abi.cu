@@ -198,6 +198,7 @@ Red Chunk::red() const {
 static void free_chunk(Chunk& c) {
   if (!c.ready) return;
   resident_release();
+  mixed_release();
   Field* l[] = {&c.density, &c.energy0, &c.energy1, &c.volume, &c.u, &c.u0,
                 &c.p,       &c.r,       &c.w,       &c.Mi,     &c.Kx, &c.Ky,
                 &c.sd,      &c.z,       &c.cp,      &c.bfp,    &c.diag};

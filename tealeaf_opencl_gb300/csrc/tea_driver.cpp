@@ -57,6 +57,10 @@ struct Deck {
   int test_problem = 0;
   bool verbose = false;
   bool fused = true;  // tl_arithmetic
+  bool mixed = false;        // tl_mixed_precision
+  bool true_exit = false;    // tl_exit_true_residual (resident CG only)
+  double mixed_inner_eps = 1e-4;
+  int mixed_max_outer = 50;
   std::vector<State> states;
 };
 
@@ -165,6 +169,16 @@ bool parse_deck(const std::string& text, Deck* D, std::string* err) {
         }
       }
       else if (w == "verbose_on") D->verbose = true;
+      else if (w == "tl_mixed_precision") {
+        // not a reference key: FP32 inner CG in FP64 defect correction
+        D->mixed = true;
+      }
+      else if (w == "tl_exit_true_residual") {
+        // not a reference key: the resident CG loop stops on ||r||_2
+        D->true_exit = true;
+      }
+      else if (w == "tl_mixed_inner_eps") ok = to_real(next(), &D->mixed_inner_eps);
+      else if (w == "tl_mixed_max_outer") ok = to_int(next(), &D->mixed_max_outer);
       else if (w == "tl_arithmetic") {
         // not a reference key: the arithmetic form of the solver kernels
         const std::string v = next();
@@ -502,6 +516,8 @@ class Driver {
     initial_residual = sqrt(initial_residual);
     if (D.verbose) say(" Initial residual %.17E\n", initial_residual);
 
+    if (D.mixed) return mixed_step(initial_residual, rx, ry);
+
     if (use_cg || use_cheby || use_ppcg) tea_leaf_cg_init_kernel_ocl_(&rro);
 
     int n = 1;
@@ -595,7 +611,8 @@ class Driver {
           if (tea::resident_cg_iterations(n, loop_max, rro,
                                           D.eps * initial_residual, &rro,
                                           &error, &n_done, &conv,
-                                          cg_alphas.data(), cg_betas.data()) != 0)
+                                          cg_alphas.data(), cg_betas.data(),
+                                          D.true_exit) != 0)
             return -1;
           n = n_done;
           if (conv) {
@@ -654,6 +671,32 @@ class Driver {
       info->inner_iterations = ppcg_inner_iters;
       info->conduction_error = error / initial_residual;
       info->exact_error = D.check_result ? exact_error / initial_residual : NAN;
+    }
+    return tea::error_code() == 0 ? 0 : -1;
+  }
+
+  // The mixed-precision solve in place of the iteration loop: FP32 CG inner
+  // solves, FP64 defect correction to tl_eps relative FP64 residual.
+  int mixed_step(double initial_residual, double rx, double ry) {
+    (void)rx;
+    (void)ry;
+    tea_gb300_mixed_info mi;
+    if (tea_gb300_mixed_solve(D.eps, D.mixed_inner_eps, D.mixed_max_outer,
+                              D.max_iters, &mi) != 0)
+      return -1;
+    say("Mixed precision: %d FP64 corrections, %lld FP32 CG iterations, "
+        "relative FP64 residual %14.7E\n",
+        mi.outer_iterations, mi.inner_iterations, mi.relative_residual);
+    tea_leaf_common_finalise_kernel_ocl_();
+    const int fe[7] = {0, 0, 1, 0, 0, 0, 0};
+    update_halo(fe, 1);
+    if (info) {
+      info->iterations = (int)mi.inner_iterations;
+      info->inner_iterations = 0;
+      info->outer_corrections = mi.outer_iterations;
+      info->relative_residual = mi.relative_residual;
+      info->conduction_error = mi.final_residual / initial_residual;
+      info->exact_error = D.check_result ? mi.final_residual / initial_residual : NAN;
     }
     return tea::error_code() == 0 ? 0 : -1;
   }

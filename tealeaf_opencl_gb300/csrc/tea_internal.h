@@ -60,6 +60,7 @@ struct ResState {
   int p_pending;  // calc_p of the current iteration still to run
   int converged;
   int pad;
+  double rr_true;  // r.r of the last iteration (true-residual exit only)
   double* alphas;  // indexed by iteration number n
   double* betas;
 };
@@ -111,6 +112,8 @@ struct Chunk {
   unsigned int* res_counter = nullptr;
   cudaGraphExec_t res_graph = nullptr;
   int res_graph_iters = 0;
+  bool res_graph_true_exit = false;
+  double res_last_rr_true = 0.0;
 
   Dev dev() const;
   Red red() const;
@@ -163,11 +166,15 @@ void launch_finalise(Chunk& c);
 void launch_field_summary(Chunk& c);
 void launch_update_halo(Chunk& c, int mask, int depth);
 // device-resident CG loop (tea_kernels.cu)
+// true_exit: stop on ||r||_2 < eps_target instead of sqrt(r.z)
 int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
                            double eps_target, double* rro_out,
                            double* error_out, int* n_done, int* converged,
-                           double* cg_alphas, double* cg_betas);
+                           double* cg_alphas, double* cg_betas,
+                           bool true_exit = false);
 void resident_release();
+// mixed-precision solve (tea_mixed.cu)
+void mixed_release();
 // FP64 fused-multiply-add instructions per second of this GPU
 double measure_fp64_rate();
 

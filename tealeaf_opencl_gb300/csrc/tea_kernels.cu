@@ -412,14 +412,16 @@ __device__ __forceinline__ double ur_update(const Dev& d, long long c,
 // finishes the reduction carries out the host steps of one CG iteration
 // (tea_solve.f90:282-330): beta = rrn/rro, rro = rrn, error = sqrt(rrn) and
 // the exit test against eps * initial_residual.
-template <int TH, bool F>
+// With NV = 2 it also sums r.r, for the device-resident loop's optional exit
+// test on the unpreconditioned residual.
+template <int TH, bool F, int NV = 1>
 __global__ void __launch_bounds__(kBlock)
     k_cg_calc_ur(Dev d, Red red, double alpha, ResState* st) {
   if (st) {
     if (*(volatile int*)&st->stop) return;
     alpha = st->rro / st->pw;
   }
-  const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+  const bool last = tile_driver<TH, NV>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (d.prec == PREC_JAC_BLOCK) {
 #pragma unroll 1
       for (int ys = y0; ys < y0 + TH; ys += 4) {
@@ -440,6 +442,7 @@ __global__ void __launch_bounds__(kBlock)
             bv = zl[i];
           }
           acc[0] = accum<F>(acc[0], av, bv);
+          if (NV > 1) acc[NV - 1] = accum<F>(acc[NV - 1], av, av);
         }
       }
     } else {
@@ -460,6 +463,7 @@ __global__ void __launch_bounds__(kBlock)
           }
         }
         acc[0] = accum<F>(acc[0], av, bv);
+        if (NV > 1) acc[NV - 1] = accum<F>(acc[NV - 1], av, av);
       }
     }
   });
@@ -476,7 +480,10 @@ __global__ void __launch_bounds__(kBlock)
     const double err = sqrt(rrn);
     st->error = err;
     st->p_pending = 1;
-    if (fabs(err) < st->eps_target) {
+    const bool done = NV > 1 ? sqrt(red.result[NV - 1]) < st->eps_target
+                             : fabs(err) < st->eps_target;
+    if (NV > 1) st->rr_true = red.result[NV - 1];
+    if (done) {
       st->converged = 1;
       st->stop = 1;
     } else if (n >= st->loop_max) {
@@ -940,28 +947,36 @@ static int tile_grid(Chunk& c, void (*kernel)(KArgs...)) {
   return (int)std::max<long long>(1, std::min<long long>(c.dev().ns, cap));
 }
 
-template <int TH, bool F>
+template <int TH, bool F, int NV>
 static void enqueue_resident_iterations_t(Chunk& c, int iters) {
   const Dev d = c.dev();
   const Red red = c.red();
   const int gw = tile_grid(c, k_cg_calc_w<TH, F>);
-  const int gu = tile_grid(c, k_cg_calc_ur<TH, F>);
+  const int gu = tile_grid(c, k_cg_calc_ur<TH, F, NV>);
   const int gp = tile_grid(c, k_cg_calc_p<TH, F>);
   for (int i = 0; i < iters; i++) {
     k_cg_calc_w<TH, F><<<gw, kBlock, 0, c.stream>>>(d, red, c.res_state);
-    k_cg_calc_ur<TH, F><<<gu, kBlock, 0, c.stream>>>(d, red, 0.0, c.res_state);
+    k_cg_calc_ur<TH, F, NV><<<gu, kBlock, 0, c.stream>>>(d, red, 0.0, c.res_state);
     k_cg_calc_p<TH, F><<<gp, kBlock, 0, c.stream>>>(d, red, 0.0, c.res_state,
                                                     c.res_counter);
   }
 }
 
-static void enqueue_resident_iterations(Chunk& c, int iters) {
+template <int NV>
+static void enqueue_resident_iterations_nv(Chunk& c, int iters) {
   if (c.TH == 16)
-    c.fused ? enqueue_resident_iterations_t<16, true>(c, iters)
-            : enqueue_resident_iterations_t<16, false>(c, iters);
+    c.fused ? enqueue_resident_iterations_t<16, true, NV>(c, iters)
+            : enqueue_resident_iterations_t<16, false, NV>(c, iters);
   else
-    c.fused ? enqueue_resident_iterations_t<4, true>(c, iters)
-            : enqueue_resident_iterations_t<4, false>(c, iters);
+    c.fused ? enqueue_resident_iterations_t<4, true, NV>(c, iters)
+            : enqueue_resident_iterations_t<4, false, NV>(c, iters);
+}
+
+static void enqueue_resident_iterations(Chunk& c, int iters, bool true_exit) {
+  if (true_exit)
+    enqueue_resident_iterations_nv<2>(c, iters);
+  else
+    enqueue_resident_iterations_nv<1>(c, iters);
 }
 
 void resident_release() {
@@ -989,8 +1004,12 @@ void resident_release() {
 int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
                            double eps_target, double* rro_out,
                            double* error_out, int* n_done, int* converged,
-                           double* cg_alphas, double* cg_betas) {
+                           double* cg_alphas, double* cg_betas, bool true_exit) {
   Chunk& c = chunk();
+  if (c.res_graph && c.res_graph_true_exit != true_exit) {
+    cudaGraphExecDestroy(c.res_graph);
+    c.res_graph = nullptr;
+  }
   const int batch = 16;
   if (c.res_coef_n < loop_max + 2) {
     cudaFree(c.res_coef);
@@ -1026,12 +1045,13 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
     if (!check_cuda(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal),
                     "graph capture"))
       return -1;
-    enqueue_resident_iterations(c, batch);
+    enqueue_resident_iterations(c, batch, true_exit);
     if (!check_cuda(cudaStreamEndCapture(c.stream, &graph), "graph capture end") ||
         !check_cuda(cudaGraphInstantiate(&c.res_graph, graph, 0), "graph instantiate"))
       return -1;
     cudaGraphDestroy(graph);
     c.res_graph_iters = batch;
+    c.res_graph_true_exit = true_exit;
   }
   // every batch runs at least one iteration until the loop stops, so the
   // loop needs at most this many batches; more means the state is corrupt
@@ -1045,7 +1065,7 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
       if (!check_cuda(cudaGraphLaunch(c.res_graph, c.stream), "graph launch"))
         return -1;
     } else {
-      enqueue_resident_iterations(c, batch);
+      enqueue_resident_iterations(c, batch, true_exit);
       check_cuda(cudaGetLastError(), "resident launch");
     }
     for (int i = 0; i < 3 * batch; i++) count_launch("resident_cg");
@@ -1058,6 +1078,7 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
   }
   *rro_out = h.rro;
   *error_out = h.error;
+  c.res_last_rr_true = h.rr_true;
   *n_done = h.n;
   *converged = h.converged;
   if (cg_alphas && cg_betas) {

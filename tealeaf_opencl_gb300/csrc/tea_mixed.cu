@@ -1,0 +1,401 @@
+// Mixed-precision implicit solve: FP32 inner CG inside an FP64
+// defect-correction loop.
+//
+//   r = u0 - A u            FP64 (the outer residual, on the FP64 fields)
+//   repeat until ||r||_2 <= tol * ||r_first||_2:
+//     solve A d = r approximately with diagonally preconditioned CG in FP32
+//       (FP32 copies of Kx, Ky, the diagonal and its inverse; FP32 vectors
+//        d, r, p, w; every dot product accumulated in FP64)
+//     u = u + d             FP64
+//     r = u0 - A u          FP64
+//
+// On GB300 the FP64 pipe bounds the FP64 stencils while FP32 stencils run at
+// HBM speed with half the bytes, so each inner iteration costs a fraction
+// of an FP64 CG iteration; the few FP64 residual passes keep the answer an
+// FP64 one.  The inner loop keeps its scalars on the device and runs in
+// batches replayed from a CUDA graph, like the FP64 resident CG loop.
+//
+// Every sum uses the fixed tile order of tea_device.cuh with lane
+// accumulation acc = fma((double)a, (double)b, acc); every FP32 expression
+// is written out with explicit fused multiply-adds, so the CPU oracle
+// (oracle_mixed_solve) reproduces the results bit for bit.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+
+#include "../../include/tealeaf_gb300.h"
+#include "tea_device.cuh"
+
+namespace tea {
+
+// FP32 fields of the mixed solve, padded like the FP64 ones (interior
+// column H of each row 256-byte aligned).
+struct MixDev {
+  long long S;  // row stride in floats
+  float *Kx, *Ky, *D, *Mi, *d, *r, *p, *w;
+};
+
+struct MixState {
+  double rro, pw, rrn, alpha, beta, rz0;
+  double eps2;  // (inner relative tolerance)^2 * rz0
+  int n, max_iters, stop, p_pending;
+  int done_iters, pad;
+};
+
+struct MixChunk {
+  bool ready = false;
+  int x_max = 0, y_max = 0, H = 0;
+  long long S = 0;
+  float* base[8] = {nullptr};
+  MixDev dev{};
+  MixState* st = nullptr;    // device
+  MixState* st_h = nullptr;  // pinned
+  unsigned int* counter = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_batch = 0;
+};
+
+static MixChunk g_mix;
+
+__device__ __forceinline__ long long cidx32(const Dev& d, const MixDev& m, int x,
+                                            int y) {
+  return (long long)(y + d.H) * m.S + (x + d.H);
+}
+
+// FP32 5-point operator with fused multiply-adds:
+// D x_c - (Ky_n x_n + Ky_c x_s) - (Kx_e x_e + Kx_c x_w)
+__device__ __forceinline__ float smvp32(const MixDev& m, const float* x,
+                                        long long c) {
+  const long long S = m.S;
+  const float kyn = __ldg(m.Ky + c + S), kyc = __ldg(m.Ky + c);
+  const float kxe = __ldg(m.Kx + c + 1), kxc = __ldg(m.Kx + c);
+  const float t1 = __fmaf_rn(kyc, x[c - S], kyn * x[c + S]);
+  const float t2 = __fmaf_rn(kxc, x[c - 1], kxe * x[c + 1]);
+  return __fmaf_rn(__ldg(m.D + c), x[c], -t1) - t2;
+}
+
+__device__ __forceinline__ double acc64(double acc, float a, float b) {
+  return __fma_rn((double)a, (double)b, acc);
+}
+
+// FP32 copies of the operator over the whole padded array:
+// Kx, Ky rounded to nearest; D and Mi = 1/D from the FP64 diagonal.
+__global__ void k_mix_convert(Dev d, MixDev m) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = blockIdx.y * blockDim.y + threadIdx.y;
+  if (col > d.xs || row > d.ys) return;
+  const long long c64 = (long long)row * d.S + col;
+  const long long c32 = (long long)row * m.S + col;
+  m.Kx[c32] = (float)d.Kx[c64];
+  m.Ky[c32] = (float)d.Ky[c64];
+  const bool in = col >= d.H && col < d.H + d.x_max && row >= d.H &&
+                  row < d.H + d.y_max;
+  const double D = in ? d.diag[c64] : 1.0;
+  m.D[c32] = (float)D;
+  m.Mi[c32] = (float)(1.0 / D);
+}
+
+// The outer step: r64 = u0 - A u (FP64, fused form), then the inner start
+// r32 = (float)r64, d = 0, z = Mi r32, p = z.  Sums: r64.r64 and r32.z.
+template <int TH>
+__global__ void __launch_bounds__(kBlock)
+    k_mix_residual(Dev d, MixDev m, Red red) {
+  tile_driver<TH, 2>(d, red, [&](int x, int y0, bool xin, double* acc) {
+#pragma unroll 2
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      double r64 = 0.0;
+      float r32 = 0.0f, z = 0.0f;
+      if (xin && y < d.y_max) {
+        const long long c = cidx(d, x, y);
+        const long long c3 = cidx32(d, m, x, y);
+        r64 = d.u0[c] - smvp<true>(d, d.u, c);
+        d.r[c] = r64;
+        r32 = (float)r64;
+        z = m.Mi[c3] * r32;
+        m.r[c3] = r32;
+        m.p[c3] = z;
+        m.d[c3] = 0.0f;
+      }
+      acc[0] = __fma_rn(r64, r64, acc[0]);
+      acc[1] = acc64(acc[1], r32, z);
+    }
+  });
+}
+
+// w = A p, sum p.w
+template <int TH>
+__global__ void __launch_bounds__(kBlock)
+    k_mix_calc_w(Dev d, MixDev m, Red red, MixState* st) {
+  if (*(volatile int*)&st->stop) return;
+  const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      float pv = 0.0f, wv = 0.0f;
+      if (xin && y < d.y_max) {
+        const long long c3 = cidx32(d, m, x, y);
+        wv = smvp32(m, m.p, c3);
+        m.w[c3] = wv;
+        pv = m.p[c3];
+      }
+      acc[0] = acc64(acc[0], pv, wv);
+    }
+  });
+  if (last && threadIdx.x == 0) st->pw = red.result[0];
+}
+
+// alpha = rro/pw; d += alpha p; r -= alpha w; z = Mi r; sum r.z; the last
+// block takes the CG scalar step and the inner exit test
+template <int TH>
+__global__ void __launch_bounds__(kBlock)
+    k_mix_calc_ur(Dev d, MixDev m, Red red, MixState* st) {
+  if (*(volatile int*)&st->stop) return;
+  const double alpha = st->rro / st->pw;
+  const float af = (float)alpha;
+  const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      float rv = 0.0f, zv = 0.0f;
+      if (xin && y < d.y_max) {
+        const long long c3 = cidx32(d, m, x, y);
+        m.d[c3] = __fmaf_rn(af, m.p[c3], m.d[c3]);
+        rv = __fmaf_rn(-af, m.w[c3], m.r[c3]);
+        m.r[c3] = rv;
+        zv = m.Mi[c3] * rv;
+      }
+      acc[0] = acc64(acc[0], rv, zv);
+    }
+  });
+  if (last && threadIdx.x == 0) {
+    const double rrn = red.result[0];
+    st->alpha = alpha;
+    st->beta = rrn / st->rro;
+    st->rrn = rrn;
+    st->rro = rrn;
+    st->p_pending = 1;
+    st->done_iters = st->n;
+    if (rrn <= st->eps2 || st->n >= st->max_iters)
+      st->stop = 1;
+    else
+      st->n = st->n + 1;
+    __threadfence();
+  }
+}
+
+// p = Mi r + beta p
+template <int TH>
+__global__ void __launch_bounds__(kBlock)
+    k_mix_calc_p(Dev d, MixDev m, Red red, MixState* st, unsigned int* counter) {
+  if (!*(volatile int*)&st->p_pending) return;
+  const float bf = (float)st->beta;
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      if (y < d.y_max) {
+        const long long c3 = cidx32(d, m, x, y);
+        m.p[c3] = __fmaf_rn(bf, m.p[c3], m.Mi[c3] * m.r[c3]);
+      }
+    }
+  });
+  if (last_block(counter) && threadIdx.x == 0) {
+    st->p_pending = 0;
+    __threadfence();
+  }
+}
+
+// u = u + d (FP64 accumulation of the FP32 correction)
+template <int TH>
+__global__ void __launch_bounds__(kBlock) k_mix_update_u(Dev d, MixDev m, Red red) {
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      if (y < d.y_max) {
+        const long long c = cidx(d, x, y);
+        d.u[c] = d.u[c] + (double)m.d[cidx32(d, m, x, y)];
+      }
+    }
+  });
+}
+
+template <class... KArgs>
+static int mix_grid(Chunk& c, void (*kernel)(KArgs...)) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, (const void*)kernel, kBlock, 0) !=
+          cudaSuccess ||
+      n < 1)
+    n = 1;
+  const long long cap = (long long)c.num_sms * n;
+  return (int)std::max<long long>(1, std::min<long long>(c.dev().ns, cap));
+}
+
+template <int TH>
+static void enqueue_inner(Chunk& c, int iters) {
+  const Dev d = c.dev();
+  const Red red = c.red();
+  const MixDev m = g_mix.dev;
+  const int gw = mix_grid(c, k_mix_calc_w<TH>);
+  const int gu = mix_grid(c, k_mix_calc_ur<TH>);
+  const int gp = mix_grid(c, k_mix_calc_p<TH>);
+  for (int i = 0; i < iters; i++) {
+    k_mix_calc_w<TH><<<gw, kBlock, 0, c.stream>>>(d, m, red, g_mix.st);
+    k_mix_calc_ur<TH><<<gu, kBlock, 0, c.stream>>>(d, m, red, g_mix.st);
+    k_mix_calc_p<TH><<<gp, kBlock, 0, c.stream>>>(d, m, red, g_mix.st, g_mix.counter);
+  }
+}
+
+void mixed_release() {
+  MixChunk& g = g_mix;
+  if (g.graph) cudaGraphExecDestroy(g.graph);
+  for (float*& b : g.base) {
+    cudaFree(b);
+    b = nullptr;
+  }
+  cudaFree(g.st);
+  cudaFree(g.counter);
+  cudaFreeHost(g.st_h);
+  g = MixChunk();
+}
+
+static bool mixed_alloc(Chunk& c) {
+  MixChunk& g = g_mix;
+  if (g.ready && g.x_max == c.x_max && g.y_max == c.y_max && g.H == c.H) return true;
+  mixed_release();
+  g.x_max = c.x_max;
+  g.y_max = c.y_max;
+  g.H = c.H;
+  g.S = ((long long)(c.x_max + 2 * c.H + 1 + 63) / 64) * 64;
+  const long long off = (64 - (c.H % 64)) % 64;
+  const size_t n = (size_t)(off + (c.y_max + 2 * c.H + 1) * g.S + 64);
+  float** f[8] = {&g.dev.Kx, &g.dev.Ky, &g.dev.D, &g.dev.Mi,
+                  &g.dev.d,  &g.dev.r,  &g.dev.p, &g.dev.w};
+  for (int i = 0; i < 8; i++) {
+    if (!check_cuda(cudaMalloc(&g.base[i], n * sizeof(float)), "cudaMalloc mixed field"))
+      return false;
+    cudaMemsetAsync(g.base[i], 0, n * sizeof(float), c.stream);
+    *f[i] = g.base[i] + off;
+  }
+  g.dev.S = g.S;
+  if (!check_cuda(cudaMalloc(&g.st, sizeof(MixState)), "cudaMalloc mixed state") ||
+      !check_cuda(cudaMallocHost(&g.st_h, sizeof(MixState)), "cudaMallocHost") ||
+      !check_cuda(cudaMalloc(&g.counter, sizeof(unsigned int)), "cudaMalloc counter"))
+    return false;
+  cudaMemsetAsync(g.counter, 0, sizeof(unsigned int), c.stream);
+  g.ready = true;
+  return true;
+}
+
+template <int TH>
+static bool mixed_solve_t(Chunk& c, double tol, double inner_tol, int max_outer,
+                          int max_inner, tea_gb300_mixed_info* info) {
+  MixChunk& g = g_mix;
+  const Dev d = c.dev();
+  const Red red = c.red();
+  const int batch = 16;
+  {
+    const dim3 block(32, 8), grid((d.xs + 1 + 31) / 32, (d.ys + 1 + 7) / 8);
+    k_mix_convert<<<grid, block, 0, c.stream>>>(d, g.dev);
+    count_launch("mixed_convert");
+  }
+  if (!g.graph) {
+    cudaGraph_t graph = nullptr;
+    if (!check_cuda(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal),
+                    "mixed graph capture"))
+      return false;
+    enqueue_inner<TH>(c, batch);
+    if (!check_cuda(cudaStreamEndCapture(c.stream, &graph), "mixed graph capture end") ||
+        !check_cuda(cudaGraphInstantiate(&g.graph, graph, 0), "mixed graph instantiate"))
+      return false;
+    cudaGraphDestroy(graph);
+    g.graph_batch = batch;
+  }
+  double res[2];
+  auto outer_residual = [&](double* out) -> bool {
+    k_mix_residual<TH><<<mix_grid(c, k_mix_residual<TH>), kBlock, 0, c.stream>>>(d, g.dev, red);
+    count_launch("mixed_residual");
+    if (!check_cuda(cudaMemcpyAsync(c.host_result, c.red_result, 2 * sizeof(double),
+                                    cudaMemcpyDeviceToHost, c.stream),
+                    "mixed residual read") ||
+        !check_cuda(cudaStreamSynchronize(c.stream), "mixed residual sync"))
+      return false;
+    out[0] = c.host_result[0];
+    out[1] = c.host_result[1];
+    return true;
+  };
+  if (!outer_residual(res)) return false;
+  const double rr_first = res[0];
+  info->initial_residual = sqrt(rr_first);
+  int outer = 0;
+  long long inner_total = 0;
+  while (!(sqrt(res[0]) <= tol * sqrt(rr_first)) && outer < max_outer) {
+    MixState& h = *g.st_h;
+    memset(&h, 0, sizeof(h));
+    h.rro = res[1];
+    h.rz0 = res[1];
+    // the last corrections only need the reduction still missing (with a
+    // margin of 4), never less than inner_tol
+    const double need = 0.25 * tol * sqrt(rr_first) / sqrt(res[0]);
+    const double itol = need > inner_tol ? (need < 0.5 ? need : 0.5) : inner_tol;
+    h.eps2 = itol * itol * res[1];
+    h.n = 1;
+    h.max_iters = max_inner;
+    if (!check_cuda(cudaMemcpyAsync(g.st, &h, sizeof(MixState), cudaMemcpyHostToDevice,
+                                    c.stream),
+                    "mixed state upload"))
+      return false;
+    const long long max_batches = max_inner / batch + 3;
+    for (long long nb = 0;; nb++) {
+      if (nb >= max_batches) {
+        fail(40, "mixed inner loop did not stop after %lld batches", nb);
+        return false;
+      }
+      if (!check_cuda(cudaGraphLaunch(g.graph, c.stream), "mixed graph launch")) return false;
+      for (int i = 0; i < 3 * batch; i++) count_launch("mixed_inner");
+      if (!check_cuda(cudaMemcpyAsync(&h, g.st, sizeof(MixState), cudaMemcpyDeviceToHost,
+                                      c.stream),
+                      "mixed state read") ||
+          !check_cuda(cudaStreamSynchronize(c.stream), "mixed sync"))
+        return false;
+      if (h.stop && !h.p_pending) break;
+    }
+    inner_total += h.done_iters;
+    k_mix_update_u<TH><<<mix_grid(c, k_mix_update_u<TH>), kBlock, 0, c.stream>>>(d, g.dev, red);
+    count_launch("mixed_update_u");
+    outer++;
+    if (!outer_residual(res)) return false;
+  }
+  info->outer_iterations = outer;
+  info->inner_iterations = inner_total;
+  info->final_residual = sqrt(res[0]);
+  info->relative_residual = sqrt(res[0]) / sqrt(rr_first);
+  return true;
+}
+
+}  // namespace tea
+
+using namespace tea;
+
+extern "C" int tea_gb300_mixed_solve(double tol, double inner_tol, int max_outer,
+                                     int max_inner, tea_gb300_mixed_info* info) {
+  Chunk& c = chunk();
+  if (!c.ready) {
+    fail(5, "tea_gb300_mixed_solve called before initialise_ocl_");
+    return -1;
+  }
+  if (!(tol > 0.0) || !(inner_tol > 0.0) || inner_tol >= 1.0 || max_outer < 1 ||
+      max_inner < 1 || !info) {
+    fail(41, "tea_gb300_mixed_solve: invalid arguments");
+    return -1;
+  }
+  memset(info, 0, sizeof(*info));
+  if (!mixed_alloc(c)) return -1;
+  const bool ok = c.TH == 16 ? mixed_solve_t<16>(c, tol, inner_tol, max_outer, max_inner, info)
+                             : mixed_solve_t<4>(c, tol, inner_tol, max_outer, max_inner, info);
+  return ok ? 0 : -1;
+}

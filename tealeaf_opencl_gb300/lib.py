@@ -42,7 +42,7 @@ EXTRA_SYMBOLS = [
     "tea_gb300_synchronize", "tea_gb300_host_alloc", "tea_gb300_host_free",
     "tea_gb300_kernel_timer_select", "tea_gb300_kernel_timer_read",
     "tea_gb300_kernel_timer_read_name", "tea_gb300_fp64_rate",
-    "tea_gb300_dot_noalloc",
+    "tea_gb300_dot_noalloc", "tea_gb300_mixed_solve",
     "tea_gb300_driver_open", "tea_gb300_driver_step", "tea_gb300_driver_close",
 ]
 
@@ -55,10 +55,19 @@ class StepInfo(C.Structure):
         ("summary_done", C.c_int), ("vol", C.c_double), ("mass", C.c_double),
         ("ie", C.c_double), ("temp", C.c_double), ("complete", C.c_int),
         ("qa_passed", C.c_int), ("qa_diff", C.c_double),
+        ("outer_corrections", C.c_int), ("relative_residual", C.c_double),
     ]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class MixedInfo(C.Structure):
+    _fields_ = [
+        ("outer_iterations", C.c_int), ("inner_iterations", C.c_longlong),
+        ("initial_residual", C.c_double), ("final_residual", C.c_double),
+        ("relative_residual", C.c_double),
+    ]
 
 
 class TeaError(RuntimeError):
@@ -133,6 +142,7 @@ def load(build=True):
         "tea_gb300_fp64_rate": (d, []),
         "tea_gb300_dot_noalloc": (i, [C.c_void_p, C.c_void_p, i, i, i, C.c_longlong,
                                       C.c_void_p, C.c_void_p]),
+        "tea_gb300_mixed_solve": (i, [d, d, i, i, C.POINTER(MixedInfo)]),
         "tea_gb300_driver_open": (i, [C.c_char_p, C.c_char_p, i, i]),
         "tea_gb300_driver_step": (i, [C.POINTER(StepInfo)]),
         "tea_gb300_driver_close": (v, []),
@@ -278,6 +288,14 @@ class Chunk:
         check()
         return tuple(o.value for o in out)
 
+    def mixed_solve(self, tol, inner_tol=1e-4, max_outer=50, max_inner=10000):
+        info = MixedInfo()
+        if load().tea_gb300_mixed_solve(tol, inner_tol, max_outer, max_inner,
+                                        C.byref(info)) != 0:
+            check()
+            raise TeaError("mixed solve failed")
+        return info
+
     def update_halo(self, fields, depth):
         f = np.ascontiguousarray(fields, dtype=np.int32)
         load().update_halo_kernel_ocl_(_pi(self.neighbours), _pi(f), _ip(depth))
@@ -307,6 +325,31 @@ class Chunk:
         assert a.shape == (self.y_max + 2 * self.halo, self.x_max + 2 * self.halo)
         if load().tea_gb300_write_field_padded(FIELD[name], _pd(a)) != 0:
             check()
+
+
+def chunk_shape():
+    """(x_max, y_max, halo, stride) of the current chunk."""
+    v = [C.c_int() for _ in range(4)]
+    if load().tea_gb300_chunk_info(*[C.byref(x) for x in v]) != 0:
+        raise TeaError("no chunk")
+    return tuple(x.value for x in v)
+
+
+def read_field(name):
+    """Interior of a field of the current chunk (y_max x x_max)."""
+    x, y, _, _ = chunk_shape()
+    out = np.zeros((y, x))
+    if load().tea_gb300_read_field(FIELD[name], _pd(out)) != 0:
+        check()
+    return out
+
+
+def write_field(name, arr):
+    x, y, _, _ = chunk_shape()
+    a = np.ascontiguousarray(arr, dtype=np.float64)
+    assert a.shape == (y, x)
+    if load().tea_gb300_write_field(FIELD[name], _pd(a)) != 0:
+        check()
 
 
 class Driver:
