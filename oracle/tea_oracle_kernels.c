@@ -104,6 +104,21 @@ static inline double lane_acc(double acc, double a, double b, int fused) {
   return fused ? fma(a, b, acc) : acc + a * b;
 }
 
+/* (hi, lo) += a*b for float a, b: the product split exactly into p + e
+ * with e = fmaf(a, b, -p), p added with a two-sum (the mixed solve's lane
+ * accumulation). */
+static inline void acc_pair(float* hi, float* lo, float a, float b) {
+  const float p = a * b;
+  const float e = fmaf(a, b, -p);
+  const float s = *hi + p;
+  const float bb = s - *hi;
+  const float t = (*hi - (s - bb)) + (p - bb);
+  *lo = *lo + (t + e);
+  *hi = s;
+}
+
+#define LANE_FLOAT_PAIR 2 /* reduce_pairs mode for FP32 products */
+
 static double reduce_pairs(const double* A, const double* B, int X, int Y,
                            int fused) {
   const int TH = oracle_reduction_rows(X, Y);
@@ -126,14 +141,18 @@ static double reduce_pairs(const double* A, const double* B, int X, int Y,
       for (int l = 0; l < 32; l++) {
         const long col = 32 * tx + l;
         double acc = 0.0;
+        float hi = 0.0f, lo = 0.0f;
         for (int j = 0; j < TH; j++) {
           const long row = (long)TH * sy + j;
           const int in = col < X && row < Y;
           const double a = in ? A[row * X + col] : 0.0;
           const double b = in ? (B ? B[row * X + col] : 1.0) : 0.0;
-          acc = lane_acc(acc, a, b, fused);
+          if (fused == LANE_FLOAT_PAIR)
+            acc_pair(&hi, &lo, (float)a, (float)b);
+          else
+            acc = lane_acc(acc, a, b, fused);
         }
-        lanes[l] = acc;
+        lanes[l] = fused == LANE_FLOAT_PAIR ? (double)hi + (double)lo : acc;
       }
       t8[wv] = butterfly32(lanes);
     }
@@ -951,8 +970,8 @@ int oracle_num_threads(void) {
  * Restates tea_gb300_mixed_solve of the CUDA library (the oracle has no
  * reference counterpart for it: it is an addition to the reference's
  * solvers).  FP32 parts use float with fmaf where the CUDA code uses
- * __fmaf_rn; FP64 parts use the fused form; every sum is reduce_pairs with
- * fma accumulation.
+ * __fmaf_rn; FP64 parts use the fused form; FP32 dot products accumulate
+ * per lane as an exact float pair (acc_pair), FP64 ones with fma.
  */
 typedef struct {
   float *Kx, *Ky, *D, *Mi, *d, *r, *p, *w;
@@ -1017,7 +1036,8 @@ static void mix_residual(double* out) {
       DOT(1, col, row, (double)r32, (double)z);
     }
   out[0] = reduce_pairs(C.scratch[0], C.scratchb[0], C.x_max, C.y_max, 1);
-  out[1] = reduce_pairs(C.scratch[1], C.scratchb[1], C.x_max, C.y_max, 1);
+  out[1] = reduce_pairs(C.scratch[1], C.scratchb[1], C.x_max, C.y_max,
+                        LANE_FLOAT_PAIR);
 }
 
 int oracle_mixed_solve(double tol, double inner_tol, int max_outer,
@@ -1060,7 +1080,8 @@ int oracle_mixed_solve(double tol, double inner_tol, int max_outer,
           M.w[c] = wv;
           DOT(0, col, row, (double)M.p[c], (double)wv);
         }
-      const double pw = reduce_pairs(C.scratch[0], C.scratchb[0], C.x_max, C.y_max, 1);
+      const double pw = reduce_pairs(C.scratch[0], C.scratchb[0], C.x_max, C.y_max,
+                                     LANE_FLOAT_PAIR);
       const double alpha = rro / pw;
       const float af = (float)alpha;
 #pragma omp parallel for schedule(static)
@@ -1073,7 +1094,8 @@ int oracle_mixed_solve(double tol, double inner_tol, int max_outer,
           const float zv = M.Mi[c] * rv;
           DOT(0, col, row, (double)rv, (double)zv);
         }
-      const double rrn = reduce_pairs(C.scratch[0], C.scratchb[0], C.x_max, C.y_max, 1);
+      const double rrn = reduce_pairs(C.scratch[0], C.scratchb[0], C.x_max, C.y_max,
+                                      LANE_FLOAT_PAIR);
       const double beta = rrn / rro;
       rro = rrn;
       done = n;

@@ -5,7 +5,7 @@
 //   repeat until ||r||_2 <= tol * ||r_first||_2:
 //     solve A d = r approximately with diagonally preconditioned CG in FP32
 //       (FP32 copies of Kx, Ky, the diagonal and its inverse; FP32 vectors
-//        d, r, p, w; every dot product accumulated in FP64)
+//        d, r, p, w; every dot product summed exactly per lane, then in FP64)
 //     u = u + d             FP64
 //     r = u0 - A u          FP64
 //
@@ -15,8 +15,12 @@
 // FP64 one.  The inner loop keeps its scalars on the device and runs in
 // batches replayed from a CUDA graph, like the FP64 resident CG loop.
 //
-// Every sum uses the fixed tile order of tea_device.cuh with lane
-// accumulation acc = fma((double)a, (double)b, acc); every FP32 expression
+// Every sum uses the fixed tile order of tea_device.cuh.  Within a lane the
+// (at most 16) products of an FP32 dot product are accumulated exactly as
+// an unevaluated pair of floats (each product split exactly with a fused
+// multiply-add, pairs added with an error-free two-sum), and the pair is
+// converted to FP64 once per tile; everything above the lane is FP64.  This
+// keeps the FP32 kernels off GB300's slow FP64 pipe.  Every FP32 expression
 // is written out with explicit fused multiply-adds, so the CPU oracle
 // (oracle_mixed_solve) reproduces the results bit for bit.
 #include <math.h>
@@ -75,8 +79,21 @@ __device__ __forceinline__ float smvp32(const MixDev& m, const float* x,
   return __fmaf_rn(__ldg(m.D + c), x[c], -t1) - t2;
 }
 
-__device__ __forceinline__ double acc64(double acc, float a, float b) {
-  return __fma_rn((double)a, (double)b, acc);
+// (hi, lo) += a*b, exactly up to the pair's rounding: the product is split
+// into p + e with e = fma(a, b, -p), and p is added with a two-sum.
+__device__ __forceinline__ void acc_pair(float& hi, float& lo, float a,
+                                         float b) {
+  const float p = a * b;
+  const float e = __fmaf_rn(a, b, -p);
+  const float s = hi + p;
+  const float bb = s - hi;
+  const float t = (hi - (s - bb)) + (p - bb);
+  lo = lo + (t + e);
+  hi = s;
+}
+
+__device__ __forceinline__ double pair_value(float hi, float lo) {
+  return (double)hi + (double)lo;
 }
 
 // FP32 copies of the operator over the whole padded array:
@@ -102,6 +119,7 @@ template <int TH>
 __global__ void __launch_bounds__(kBlock)
     k_mix_residual(Dev d, MixDev m, Red red) {
   tile_driver<TH, 2>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    float hi = 0.0f, lo = 0.0f;
 #pragma unroll 2
     for (int j = 0; j < TH; j++) {
       const int y = y0 + j;
@@ -119,8 +137,9 @@ __global__ void __launch_bounds__(kBlock)
         m.d[c3] = 0.0f;
       }
       acc[0] = __fma_rn(r64, r64, acc[0]);
-      acc[1] = acc64(acc[1], r32, z);
+      acc_pair(hi, lo, r32, z);
     }
+    acc[1] = pair_value(hi, lo);
   });
 }
 
@@ -130,6 +149,7 @@ __global__ void __launch_bounds__(kBlock)
     k_mix_calc_w(Dev d, MixDev m, Red red, MixState* st) {
   if (*(volatile int*)&st->stop) return;
   const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    float hi = 0.0f, lo = 0.0f;
 #pragma unroll 4
     for (int j = 0; j < TH; j++) {
       const int y = y0 + j;
@@ -140,8 +160,9 @@ __global__ void __launch_bounds__(kBlock)
         m.w[c3] = wv;
         pv = m.p[c3];
       }
-      acc[0] = acc64(acc[0], pv, wv);
+      acc_pair(hi, lo, pv, wv);
     }
+    acc[0] = pair_value(hi, lo);
   });
   if (last && threadIdx.x == 0) st->pw = red.result[0];
 }
@@ -155,6 +176,7 @@ __global__ void __launch_bounds__(kBlock)
   const double alpha = st->rro / st->pw;
   const float af = (float)alpha;
   const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    float hi = 0.0f, lo = 0.0f;
 #pragma unroll 4
     for (int j = 0; j < TH; j++) {
       const int y = y0 + j;
@@ -166,8 +188,9 @@ __global__ void __launch_bounds__(kBlock)
         m.r[c3] = rv;
         zv = m.Mi[c3] * rv;
       }
-      acc[0] = acc64(acc[0], rv, zv);
+      acc_pair(hi, lo, rv, zv);
     }
+    acc[0] = pair_value(hi, lo);
   });
   if (last && threadIdx.x == 0) {
     const double rrn = red.result[0];
