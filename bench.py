@@ -443,6 +443,95 @@ def run_mixed(args):
     return out
 
 
+BATCH_BYTES_PER_CELL_ITER = 128  # CG with jac_diag: calc_w 40, calc_ur 64, calc_p 24
+
+
+def run_batch(args):
+    """Many independent problems solved together (tea_gb300_batch_*): seeded
+    problems of uneven size, FP64 CG with diagonal Jacobi, tl_eps 1e-12,
+    args.steps timesteps each.  Reports the batch's cell-iterations/s with the
+    fields reset before every timed run, and the same problems solved one
+    after another by the single-chunk resident driver on a sample."""
+    import numpy as np
+    from tealeaf_opencl_gb300 import decks, lib
+    L = lib.load()
+    L.tea_gb300_set_arithmetic(1)
+    problems = decks.batch_problems(args.problems, seed=args.seed)
+    t0 = time.perf_counter()
+    fields = [decks.paint(p) for p in problems]
+    paint_s = time.perf_counter() - t0
+    b = lib.Batch([(p["x"], p["y"]) for p in problems], prec="jac_diag")
+    cells = sum(p["x"] * p["y"] for p in problems)
+
+    def reset():
+        for i, (d, e) in enumerate(fields):
+            b.set_fields(i, d, e)
+
+    reset()
+    t0 = time.perf_counter()
+    tuned = b.autotune()
+    tune_s = time.perf_counter() - t0
+    runs = []
+    for rep in range(max(1, args.reps)):
+        reset()
+        t0 = time.perf_counter()
+        st = b.run(args.steps, 0.004, 1e-12, 5000)
+        runs.append((time.perf_counter() - t0, st.as_dict()))
+    wall, st = min(runs, key=lambda r: r[1]["total_ms"])
+    iters = np.array([b.iterations(i) for i in range(len(problems))])
+    peak, peak_kind = measured_peak_hbm()
+    rate = st["cell_iterations"] / (st["total_ms"] * 1e-3)
+    out = {"mode": "batch", "problems": len(problems), "seed": args.seed,
+           "cells": cells, "steps": args.steps, "eps": 1e-12, "prec": "jac_diag",
+           "dtype": "f64", "launch": tuned, "autotune_seconds": tune_s,
+           "paint_seconds": paint_s, "stats": st, "wall_seconds": wall,
+           "cell_iters_per_s": rate,
+           "solve_gbs": st["cell_iterations"] * BATCH_BYTES_PER_CELL_ITER / (st["solve_ms"] * 1e-3) / 1e9,
+           "hbm_peak_gbs": peak, "hbm_peak_kind": peak_kind,
+           "iterations_per_step": {"min": int(iters.min()), "median": float(np.median(iters)),
+                                   "max": int(iters.max())}}
+    out["solve_frac_of_measured_hbm"] = out["solve_gbs"] / peak if peak else None
+    b.free()
+    # the same problems one by one through the single-chunk resident driver
+    k = min(args.sequential, len(problems))
+    if k > 0:
+        seq_s, seq_ci = 0.0, 0.0
+        for p in problems[:k]:
+            deck = decks.batch_deck(p, steps=args.steps, eps=1e-12, prec="jac_diag",
+                                    arithmetic="fused")
+            drv = lib.Driver(deck, mode=lib.DRIVER_RESIDENT)
+            L.tea_gb300_synchronize()
+            t0 = time.perf_counter()
+            its = 0
+            while True:
+                info = drv.step()
+                if info is None:
+                    break
+                its += info.iterations
+                if info.complete:
+                    break
+            L.tea_gb300_synchronize()
+            seq_s += time.perf_counter() - t0
+            seq_ci += p["x"] * p["y"] * its
+            drv.close()
+        sub = lib.Batch([(p["x"], p["y"]) for p in problems[:k]], prec="jac_diag")
+        for i in range(k):
+            sub.set_fields(i, *fields[i])
+        sub.autotune()
+        for i in range(k):
+            sub.set_fields(i, *fields[i])
+        t0 = time.perf_counter()
+        sst = sub.run(args.steps, 0.004, 1e-12, 5000)
+        sub_s = time.perf_counter() - t0
+        sub.free()
+        out["sequential_sample"] = {
+            "problems": k, "single_chunk_seconds": seq_s,
+            "single_chunk_cell_iters_per_s": seq_ci / seq_s,
+            "batch_seconds": sub_s, "batch_cell_iters_per_s": sst.cell_iterations / sub_s,
+            "speedup": seq_s / sub_s}
+    return out
+
+
 def cpu_sample(name, steps_timed, cap):
     """Oracle on the same deck: one warm-up step, then steps_timed steps,
     every step capped at `cap` outer iterations; returns (value, detail)."""
@@ -503,13 +592,17 @@ def main():
     ap.add_argument("--cap", type=int, default=0,
                     help="limit solver iterations per GPU step (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="run", choices=["run", "kernels", "mixed"],
+    ap.add_argument("--mode", default="run", choices=["run", "kernels", "mixed", "batch"],
                     help="kernels: time each hot entry point on the workload's grid; "
                          "mixed: FP64 vs FP32-inner/FP64-refined CG to 1e-10")
     ap.add_argument("--cells", type=int, default=4096, help="grid side for --mode mixed")
     ap.add_argument("--lognormal", action="store_true",
                     help="--mode mixed: density times a seeded log-normal field")
     ap.add_argument("--reps", type=int, default=20)
+    ap.add_argument("--problems", type=int, default=512, help="--mode batch: problem count")
+    ap.add_argument("--seed", type=int, default=0, help="--mode batch: problem seed")
+    ap.add_argument("--sequential", type=int, default=32,
+                    help="--mode batch: problems also run one by one for comparison")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
@@ -530,6 +623,9 @@ def main():
         return
     if args.mode == "mixed":
         print(json.dumps(run_mixed(args)))
+        return
+    if args.mode == "batch":
+        print(json.dumps(run_batch(args)))
         return
 
     dist = Dist()

@@ -342,6 +342,69 @@ int tea_gb300_driver_step(tea_gb300_step_info* info);
 /* Closes the log; the chunk stays allocated for inspection. */
 void tea_gb300_driver_close(void);
 
+/* ---- batched solves (no counterpart in the reference) ----
+ *
+ * Many independent single-chunk problems of different sizes, solved
+ * together on the GPU with FP64 CG.  Each problem follows, step for step,
+ * what the driver above does for one chunk with tl_use_cg and reflective
+ * boundaries (tea_solve.f90:37-420 with all faces external): its iteration
+ * counts and field summaries are bit-identical to a single-chunk run of the
+ * same problem with the same arithmetic form.  One batch exists per process,
+ * independent of the chunk; it uses its own stream. */
+
+typedef struct {
+  int steps;                 /* timesteps run by the call */
+  int max_iterations;        /* largest per-problem iteration count of a step */
+  long long iterations;      /* sum of iterations over problems and steps */
+  double cell_iterations;    /* sum of cells x iterations */
+  int graph_launches;        /* graph replays of the iteration kernels */
+  long long kernel_launches; /* kernels run by the call (graph nodes included) */
+  double solve_ms;           /* GPU time of the iteration phase (all steps) */
+  double total_ms;           /* GPU time of the whole call */
+} tea_gb300_batch_stats;
+
+/* Launch geometry of the iteration kernels.  None of it changes a result:
+ * the summation order of every problem is fixed by its own size. */
+typedef struct {
+  int blocks_per_sm;         /* resident blocks per SM of each kernel (1..8) */
+  int graph_iterations;      /* CG iterations per graph replay (1..64) */
+  int supertiles_per_unit;   /* 256-column supertiles per work unit (1..64) */
+} tea_gb300_batch_launch;
+
+/* Creates a batch of n problems; problem i has x_cells[i] x y_cells[i]
+ * cells on [xmin,xmax] x [ymin,ymax].  preconditioner: TEA_PREC_NONE,
+ * TEA_PREC_JAC_DIAG or TEA_PREC_JAC_BLOCK; coefficient: TEA_COEF_*.  The
+ * arithmetic form is the one set by tea_gb300_set_arithmetic.  Replaces any
+ * earlier batch.  Returns 0 or -1. */
+int tea_gb300_batch_create(int n, const int* x_cells, const int* y_cells,
+                           double xmin, double xmax, double ymin, double ymax,
+                           int preconditioner, int coefficient);
+/* Sets problem i's density and energy (host arrays of x_cells*y_cells
+ * values, x fastest), as generate_chunk and set_field leave them. */
+int tea_gb300_batch_set_fields(int i, const double* density,
+                               const double* energy);
+/* Runs `steps` timesteps of length dt on every problem, each solved to
+ * ||r|| < eps ||r0|| or max_iters iterations.  stats may be NULL. */
+int tea_gb300_batch_run(int steps, double dt, double eps, int max_iters,
+                        tea_gb300_batch_stats* stats);
+/* Field summary of problem i (vol, mass, ie, temp; field_summary_kernel).  */
+int tea_gb300_batch_summary(int i, double summary[4]);
+/* Iteration count of problem i in each step of the last run
+ * (steps values). */
+int tea_gb300_batch_iterations(int i, int* iterations, int steps);
+/* Copies problem i's interior field (TEA_FIELD_DENSITY, _ENERGY1 or _U) to
+ * out (x_cells*y_cells values, x fastest). */
+int tea_gb300_batch_read_field(int i, int field, double* out);
+/* Sets / reads the launch geometry. */
+int tea_gb300_batch_set_launch(const tea_gb300_batch_launch* launch);
+int tea_gb300_batch_get_launch(tea_gb300_batch_launch* launch);
+/* Times one CG iteration phase per candidate geometry on the batch's
+ * current state (restored afterwards) and keeps the fastest; best gets the
+ * choice.  The fields and every later result are unchanged by the search. */
+int tea_gb300_batch_autotune(tea_gb300_batch_launch* best);
+/* Releases the batch. */
+void tea_gb300_batch_free(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,7 @@ bool check_cuda(cudaError_t e, const char* what) {
 }
 
 void count_launch(const char*) { g_launches++; }
+void count_launches(long long n) { g_launches += n; }
 
 struct ProfEntry {
   long long calls = 0;
@@ -157,6 +158,7 @@ Dev Chunk::dev() const {
   d.nsx = (d.ntx + kTilesPerSuper - 1) / kTilesPerSuper;
   d.nty = (y_max + TH - 1) / TH;
   d.ns = d.nsx * d.nty;
+  d.th = TH;
   d.density = density.f;
   d.energy0 = energy0.f;
   d.energy1 = energy1.f;

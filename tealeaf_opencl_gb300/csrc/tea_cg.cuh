@@ -1,0 +1,169 @@
+// CG tile bodies shared by the single-chunk kernels (tea_kernels.cu) and
+// the batched kernels (tea_batch.cu): one lane's column x of one tile,
+// rows y0 .. y0+TH-1, with the arithmetic of the reference kernels.
+#pragma once
+
+#include "tea_device.cuh"
+
+namespace tea {
+
+// Every tile body below works in groups of 4 rows and, within a group,
+// issues all of its loads before its first store.  The fields are reached
+// through the members of Dev, which the compiler must assume may alias, so
+// a load written after a store cannot move above it; loading the group
+// first keeps 4 rows of loads in flight instead of one.  The arithmetic and
+// the order of the per-lane sums are those of the row-by-row form.
+
+// w = A p and the lane's share of p.w (tea_leaf_cg_cl.cl:45-69)
+template <int TH, bool F>
+__device__ __forceinline__ void cg_w_tile(const Dev& d, int x, int y0, bool xin,
+                                          double* acc) {
+#pragma unroll 1
+  for (int g = y0; g < y0 + TH; g += 4) {
+    const long long c0 = cidx(d, x, g);
+    double pv[4], wv[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      pv[j] = 0.0;
+      wv[j] = 0.0;
+      if (xin && g + j < d.y_max) {
+        wv[j] = smvp<F>(d, d.p, c0 + j * d.S);
+        pv[j] = d.p[c0 + j * d.S];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (xin && g + j < d.y_max) d.w[c0 + j * d.S] = wv[j];
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc[0] = accum<F>(acc[0], pv[j], wv[j]);
+  }
+}
+
+// u += alpha p; r -= alpha w (tea_leaf_cg_cl.cl:88-89) on loaded values
+template <bool F>
+__device__ __forceinline__ void ur_values(double alpha, double& u, double p,
+                                          double& r, double w) {
+  if (F) {
+    u = __fma_rn(alpha, p, u);
+    r = __fma_rn(-alpha, w, r);
+  } else {
+    u = u + alpha * p;
+    r = r - alpha * w;
+  }
+}
+
+// u += alpha p, r -= alpha w, z = M^-1 r and the lane's share of r.z (and
+// of r.r when NV == 2), tea_leaf_cg_cl.cl:73-137
+template <int TH, bool F, int NV>
+__device__ __forceinline__ void cg_ur_tile(const Dev& d, int x, int y0, bool xin,
+                                           double* acc, double alpha) {
+#pragma unroll 1
+  for (int g = y0; g < y0 + TH; g += 4) {
+    const long long c0 = cidx(d, x, g);
+    bool in[4];
+    double uv[4], pv[4], rv[4], wv[4], mv[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      in[j] = xin && g + j < d.y_max;
+      uv[j] = pv[j] = rv[j] = wv[j] = mv[j] = 0.0;
+      if (in[j]) {
+        const long long c = c0 + j * d.S;
+        uv[j] = d.u[c];
+        pv[j] = d.p[c];
+        rv[j] = d.r[c];
+        wv[j] = d.w[c];
+        if (d.prec == PREC_JAC_DIAG) mv[j] = d.Mi[c];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      if (in[j]) {
+        ur_values<F>(alpha, uv[j], pv[j], rv[j], wv[j]);
+        d.u[c0 + j * d.S] = uv[j];
+        d.r[c0 + j * d.S] = rv[j];
+      }
+    }
+    double zv[4] = {0.0, 0.0, 0.0, 0.0};
+    if (d.prec == PREC_JAC_BLOCK) {
+      // one 4-row strip of the block-Jacobi solve (strips start at rows
+      // that are multiples of 4)
+      if (in[0]) strip_solve<F>(d, c0, strip_rows(d, g), rv, zv);
+    } else if (d.prec == PREC_JAC_DIAG) {
+#pragma unroll
+      for (int j = 0; j < 4; j++) zv[j] = rv[j] * mv[j];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      double av = 0.0, bv = 0.0;
+      if (in[j]) {
+        if (d.prec != PREC_NONE) d.z[c0 + j * d.S] = zv[j];
+        av = rv[j];
+        bv = d.prec != PREC_NONE ? zv[j] : rv[j];
+      }
+      acc[0] = accum<F>(acc[0], av, bv);
+      if (NV > 1) acc[NV - 1] = accum<F>(acc[NV - 1], av, av);
+    }
+  }
+}
+
+// p = z + beta p, or r + beta p without a preconditioner
+// (tea_leaf_cg_cl.cl:141-160)
+template <int TH, bool F>
+__device__ __forceinline__ void cg_p_tile(const Dev& d, int x, int y0, bool xin,
+                                          double beta) {
+  if (!xin) return;
+  const double* src = d.prec != PREC_NONE ? d.z : d.r;
+#pragma unroll 1
+  for (int g = y0; g < y0 + TH; g += 4) {
+    const long long c0 = cidx(d, x, g);
+    double sv[4], pv[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      sv[j] = pv[j] = 0.0;
+      if (g + j < d.y_max) {
+        sv[j] = src[c0 + j * d.S];
+        pv[j] = d.p[c0 + j * d.S];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (g + j < d.y_max)
+        d.p[c0 + j * d.S] = F ? __fma_rn(beta, pv[j], sv[j]) : sv[j] + beta * pv[j];
+  }
+}
+
+// The host steps of one CG iteration (tea_solve.f90:282-330) after calc_ur,
+// on the device: beta = rrn/rro, rro = rrn, error = sqrt(rrn), and the exit
+// test (on sqrt(r.z), or on ||r||_2 when NV == 2).  result[] holds the
+// reduced sums; run by one thread.
+template <int NV>
+__device__ __forceinline__ void cg_scalar_step(ResState* st, double alpha,
+                                               const double* result) {
+  const double rrn = result[0];
+  const int n = st->n;
+  const double beta = rrn / st->rro;
+  if (st->alphas) {
+    st->alphas[n] = alpha;
+    st->betas[n] = beta;
+  }
+  st->alpha = alpha;
+  st->beta = beta;
+  st->rrn = rrn;
+  st->rro = rrn;
+  const double err = sqrt(rrn);
+  st->error = err;
+  st->p_pending = 1;
+  const bool done = NV > 1 ? sqrt(result[NV - 1]) < st->eps_target
+                           : fabs(err) < st->eps_target;
+  if (NV > 1) st->rr_true = result[NV - 1];
+  if (done) {
+    st->converged = 1;
+    st->stop = 1;
+  } else if (n >= st->loop_max) {
+    st->stop = 1;
+  } else {
+    st->n = n + 1;
+  }
+}
+
+}  // namespace tea

@@ -163,6 +163,30 @@ __device__ __forceinline__ void supertile_partial(const Red& red, int s,
   __syncthreads();
 }
 
+// Step 4 of the summation order, by one whole block: the ns partials of
+// each of the NV sums (NV arrays, `stride` apart) reduced into result[v].
+template <int NV>
+__device__ __forceinline__ void block_final_sum(const double* partials,
+                                                long long stride, int ns,
+                                                double* result, double* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll 1
+  for (int v = 0; v < NV; v++) {
+    double a = 0.0;
+    for (int k = threadIdx.x; k < ns; k += kBlock)
+      a = a + __ldcg(partials + v * stride + k);
+    a = bfly(a);
+    if (lane == 0) sh[warp] = a;
+    __syncthreads();
+    if (warp == 0) {
+      double t = lane < 8 ? sh[lane] : 0.0;
+      t = bfly(t);
+      if (lane == 0) result[v] = t;
+    }
+    __syncthreads();
+  }
+}
+
 // Last-block-done finish of the reduction; returns true in the block that
 // wrote the results.
 template <int NV>
@@ -178,22 +202,7 @@ __device__ __forceinline__ bool finish_reduction(const Red& red, int ns,
   __syncthreads();
   if (!is_last) return false;
   __threadfence();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll 1
-  for (int v = 0; v < NV; v++) {
-    double a = 0.0;
-    for (int k = threadIdx.x; k < ns; k += kBlock)
-      a = a + __ldcg(red.partials + v * red.stride + k);
-    a = bfly(a);
-    if (lane == 0) sh[warp] = a;
-    __syncthreads();
-    if (warp == 0) {
-      double t = lane < 8 ? sh[lane] : 0.0;
-      t = bfly(t);
-      if (lane == 0) red.result[v] = t;
-    }
-    __syncthreads();
-  }
+  block_final_sum<NV>(red.partials, red.stride, ns, red.result, sh);
   if (threadIdx.x == 0) *red.counter = 0u;
   return true;
 }

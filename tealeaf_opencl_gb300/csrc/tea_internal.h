@@ -34,6 +34,7 @@ struct Dev {
   int prec;
   int block_top_check;  // y_max % 4 != 0 (ocl_kernels.cpp:26-29)
   int ntx, nsx, nty, ns;  // tiling for the chunk's tile height
+  int th;                 // the tile height itself (4 or 16)
   double *density, *energy0, *energy1, *volume;
   double *u, *u0, *p, *r, *w, *Mi, *Kx, *Ky, *sd, *z, *cp, *bfp, *un;
   double* diag;  // 1 + (Ky_n + Ky_c) + (Kx_e + Kx_c), set by common_init
@@ -126,6 +127,7 @@ void fail(int code, const char* fmt, ...);
 int error_code();
 bool check_cuda(cudaError_t e, const char* what);
 void count_launch(const char* name);
+void count_launches(long long n);  // n kernels run from a graph replay
 void profile_begin(const char* name);
 void profile_end(const char* name);
 
@@ -165,6 +167,29 @@ void launch_jacobi_solve(Chunk& c);
 void launch_finalise(Chunk& c);
 void launch_field_summary(Chunk& c);
 void launch_update_halo(Chunk& c, int mask, int depth);
+// The same kernels for an explicit field set (a problem of a batch):
+// launched on `stream` with grids sized for `num_sms` SMs.
+struct LaunchCtx {
+  cudaStream_t stream;
+  int num_sms;
+  bool fused;
+};
+Dev make_dev_tiling(Dev d);  // fills th, ntx, nsx, nty, ns from x_max, y_max
+void dev_volume(const LaunchCtx& l, const Dev& d, double vol);
+void dev_init_common(const LaunchCtx& l, const Dev& d, int coef, double rx,
+                     double ry);
+void dev_zero_boundary(const LaunchCtx& l, const Dev& d, const int* zb);
+void dev_init_diag(const LaunchCtx& l, const Dev& d, const Red& r);
+void dev_init_jac_diag(const LaunchCtx& l, const Dev& d);
+void dev_init_u(const LaunchCtx& l, const Dev& d, const double* energy);
+void dev_calc_residual(const LaunchCtx& l, const Dev& d, const Red& r);
+void dev_dot(const LaunchCtx& l, const Dev& d, const Red& r, const double* a,
+             const double* b);
+void dev_block_init(const LaunchCtx& l, const Dev& d);
+void dev_update_halo(const LaunchCtx& l, const Dev& d, int mask, int depth);
+void dev_cg_init_p(const LaunchCtx& l, const Dev& d, const Red& r);
+void dev_finalise(const LaunchCtx& l, const Dev& d, const Red& r);
+void dev_field_summary(const LaunchCtx& l, const Dev& d, const Red& r);
 // device-resident CG loop (tea_kernels.cu)
 // true_exit: stop on ||r||_2 < eps_target instead of sqrt(r.z)
 int resident_cg_iterations(int n_begin, int loop_max, double rro_in,

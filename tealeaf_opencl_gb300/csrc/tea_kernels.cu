@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <unordered_map>
 
+#include "tea_cg.cuh"
 #include "tea_device.cuh"
 
 namespace tea {
@@ -280,14 +281,20 @@ template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock) k_calc_residual(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
-#pragma unroll 4
-    for (int j = 0; j < TH; j++) {
-      const int y = y0 + j;
-      if (y < d.y_max) {
-        const long long c = cidx(d, x, y);
-        const double s = smvp<F>(d, d.u, c);
-        d.r[c] = d.u0[c] - s;
-      }
+#pragma unroll 1
+    for (int g = y0; g < y0 + TH; g += 4) {
+      const long long c0 = cidx(d, x, g);
+      double rv[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (g + j < d.y_max) {
+          const long long c = c0 + j * d.S;
+          const double s = smvp<F>(d, d.u, c);
+          rv[j] = d.u0[c] - s;
+        }
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (g + j < d.y_max) d.r[c0 + j * d.S] = rv[j];
     }
   });
 }
@@ -342,25 +349,26 @@ __global__ void __launch_bounds__(kBlock) k_cg_init_p(Dev d, Red red) {
         }
       }
     } else {
-#pragma unroll 4
-      for (int j = 0; j < TH; j++) {
-        const int y = y0 + j;
-        double av = 0.0, bv = 0.0;
-        if (xin && y < d.y_max) {
-          const long long c = cidx(d, x, y);
-          const double rv = d.r[c];
-          double pv;
-          if (d.prec == PREC_JAC_DIAG) {
-            pv = rv * d.Mi[c];
-            d.z[c] = pv;
-          } else {
-            pv = rv;
+#pragma unroll 1
+      for (int g = y0; g < y0 + TH; g += 4) {
+        const long long c0 = cidx(d, x, g);
+        double rv[4], pv[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          rv[j] = pv[j] = 0.0;
+          if (xin && g + j < d.y_max) {
+            rv[j] = d.r[c0 + j * d.S];
+            pv[j] = d.prec == PREC_JAC_DIAG ? rv[j] * d.Mi[c0 + j * d.S] : rv[j];
           }
-          d.p[c] = pv;
-          av = rv;
-          bv = pv;
         }
-        acc[0] = accum<F>(acc[0], av, bv);
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          if (xin && g + j < d.y_max) {
+            if (d.prec == PREC_JAC_DIAG) d.z[c0 + j * d.S] = pv[j];
+            d.p[c0 + j * d.S] = pv[j];
+          }
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[0] = accum<F>(acc[0], rv[j], pv[j]);
       }
     }
   });
@@ -374,46 +382,16 @@ __global__ void __launch_bounds__(kBlock)
     k_cg_calc_w(Dev d, Red red, ResState* st) {
   if (st && *(volatile int*)&st->stop) return;
   const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
-#pragma unroll 4
-    for (int j = 0; j < TH; j++) {
-      const int y = y0 + j;
-      double av = 0.0, bv = 0.0;
-      if (xin && y < d.y_max) {
-        const long long c = cidx(d, x, y);
-        const double wv = smvp<F>(d, d.p, c);
-        d.w[c] = wv;
-        av = d.p[c];
-        bv = wv;
-      }
-      acc[0] = accum<F>(acc[0], av, bv);
-    }
+    cg_w_tile<TH, F>(d, x, y0, xin, acc);
   });
   if (st && last && threadIdx.x == 0) st->pw = red.result[0];
-}
-
-// u += alpha p; r -= alpha w (tea_leaf_cg_cl.cl:88-89), returns the new r
-template <bool F>
-__device__ __forceinline__ double ur_update(const Dev& d, long long c,
-                                            double alpha) {
-  if (F) {
-    d.u[c] = __fma_rn(alpha, d.p[c], d.u[c]);
-    const double rv = __fma_rn(-alpha, d.w[c], d.r[c]);
-    d.r[c] = rv;
-    return rv;
-  }
-  d.u[c] = d.u[c] + alpha * d.p[c];
-  const double rv = d.r[c] - alpha * d.w[c];
-  d.r[c] = rv;
-  return rv;
 }
 
 // tea_leaf_cg_solve_calc_ur, tea_leaf_cg_cl.cl:73-137.  In the
 // device-resident loop alpha = rro/pw is formed here, and the block that
 // finishes the reduction carries out the host steps of one CG iteration
-// (tea_solve.f90:282-330): beta = rrn/rro, rro = rrn, error = sqrt(rrn) and
-// the exit test against eps * initial_residual.
-// With NV = 2 it also sums r.r, for the device-resident loop's optional exit
-// test on the unpreconditioned residual.
+// (cg_scalar_step).  With NV = 2 it also sums r.r, for the resident loop's
+// optional exit test on the unpreconditioned residual.
 template <int TH, bool F, int NV = 1>
 __global__ void __launch_bounds__(kBlock)
     k_cg_calc_ur(Dev d, Red red, double alpha, ResState* st) {
@@ -422,75 +400,10 @@ __global__ void __launch_bounds__(kBlock)
     alpha = st->rro / st->pw;
   }
   const bool last = tile_driver<TH, NV>(d, red, [&](int x, int y0, bool xin, double* acc) {
-    if (d.prec == PREC_JAC_BLOCK) {
-#pragma unroll 1
-      for (int ys = y0; ys < y0 + TH; ys += 4) {
-        double zl[4] = {0.0, 0.0, 0.0, 0.0}, rl[4] = {0.0, 0.0, 0.0, 0.0};
-        const long long c0 = cidx(d, x, ys);
-        if (xin && ys < d.y_max) {
-#pragma unroll
-          for (int i = 0; i < 4; i++)
-            if (ys + i < d.y_max) rl[i] = ur_update<F>(d, c0 + i * d.S, alpha);
-          strip_solve<F>(d, c0, strip_rows(d, ys), rl, zl);
-        }
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-          double av = 0.0, bv = 0.0;
-          if (xin && ys + i < d.y_max) {
-            d.z[c0 + i * d.S] = zl[i];
-            av = rl[i];
-            bv = zl[i];
-          }
-          acc[0] = accum<F>(acc[0], av, bv);
-          if (NV > 1) acc[NV - 1] = accum<F>(acc[NV - 1], av, av);
-        }
-      }
-    } else {
-#pragma unroll 4
-      for (int j = 0; j < TH; j++) {
-        const int y = y0 + j;
-        double av = 0.0, bv = 0.0;
-        if (xin && y < d.y_max) {
-          const long long c = cidx(d, x, y);
-          const double rv = ur_update<F>(d, c, alpha);
-          av = rv;
-          if (d.prec == PREC_JAC_DIAG) {
-            const double zv = rv * d.Mi[c];
-            d.z[c] = zv;
-            bv = zv;
-          } else {
-            bv = rv;
-          }
-        }
-        acc[0] = accum<F>(acc[0], av, bv);
-        if (NV > 1) acc[NV - 1] = accum<F>(acc[NV - 1], av, av);
-      }
-    }
+    cg_ur_tile<TH, F, NV>(d, x, y0, xin, acc, alpha);
   });
   if (st && last && threadIdx.x == 0) {
-    const double rrn = red.result[0];
-    const int n = st->n;
-    const double beta = rrn / st->rro;
-    st->alphas[n] = alpha;
-    st->betas[n] = beta;
-    st->alpha = alpha;
-    st->beta = beta;
-    st->rrn = rrn;
-    st->rro = rrn;
-    const double err = sqrt(rrn);
-    st->error = err;
-    st->p_pending = 1;
-    const bool done = NV > 1 ? sqrt(red.result[NV - 1]) < st->eps_target
-                             : fabs(err) < st->eps_target;
-    if (NV > 1) st->rr_true = red.result[NV - 1];
-    if (done) {
-      st->converged = 1;
-      st->stop = 1;
-    } else if (n >= st->loop_max) {
-      st->stop = 1;
-    } else {
-      st->n = n + 1;
-    }
+    cg_scalar_step<NV>(st, alpha, red.result);
     __threadfence();
   }
 }
@@ -507,16 +420,7 @@ __global__ void __launch_bounds__(kBlock)
     beta = st->beta;
   }
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
-    if (!xin) return;
-    const double* src = d.prec != PREC_NONE ? d.z : d.r;
-#pragma unroll 4
-    for (int j = 0; j < TH; j++) {
-      const int y = y0 + j;
-      if (y < d.y_max) {
-        const long long c = cidx(d, x, y);
-        d.p[c] = F ? __fma_rn(beta, d.p[c], src[c]) : src[c] + beta * d.p[c];
-      }
-    }
+    cg_p_tile<TH, F>(d, x, y0, xin, beta);
   });
   if (st && last_block(counter) && threadIdx.x == 0) {
     st->p_pending = 0;
@@ -547,17 +451,22 @@ __global__ void __launch_bounds__(kBlock)
     if (d.prec == PREC_JAC_BLOCK) {
 #pragma unroll 1
       for (int ys = y0; ys < y0 + TH && ys < d.y_max; ys += 4) {
-        double zl[4], rl[4] = {0.0, 0.0, 0.0, 0.0};
+        double zl[4], rl[4] = {0.0, 0.0, 0.0, 0.0}, wl[4], pl[4];
         const long long c0 = cidx(d, x, ys);
 #pragma unroll
         for (int i = 0; i < 4; i++) {
           if (ys + i < d.y_max) {
             const long long c = c0 + i * d.S;
-            const double wv = smvp<F>(d, d.u, c);
-            d.w[c] = wv;
-            const double rv = d.u0[c] - wv;
-            d.r[c] = rv;
-            rl[i] = rv;
+            wl[i] = smvp<F>(d, d.u, c);
+            rl[i] = d.u0[c] - wl[i];
+            if (mode != 0) pl[i] = d.p[c];
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          if (ys + i < d.y_max) {
+            d.w[c0 + i * d.S] = wl[i];
+            d.r[c0 + i * d.S] = rl[i];
           }
         }
         strip_solve<F>(d, c0, strip_rows(d, ys), rl, zl);
@@ -568,30 +477,43 @@ __global__ void __launch_bounds__(kBlock)
             if (mode == 0)
               d.p[c] = zl[i] / theta;
             else
-              d.p[c] = cheby_update<F>(alpha, d.p[c], beta, zl[i]);
+              d.p[c] = cheby_update<F>(alpha, pl[i], beta, zl[i]);
           }
         }
       }
     } else {
-#pragma unroll 4
-      for (int j = 0; j < TH; j++) {
-        const int y = y0 + j;
-        if (y < d.y_max) {
-          const long long c = cidx(d, x, y);
-          const double wv = smvp<F>(d, d.u, c);
-          d.w[c] = wv;
-          const double rv = d.u0[c] - wv;
-          d.r[c] = rv;
-          if (mode == 0) {
-            if (d.prec == PREC_JAC_DIAG)
-              d.p[c] = (d.Mi[c] * rv) / theta;
-            else
-              d.p[c] = rv / theta;
-          } else {
-            if (d.prec == PREC_JAC_DIAG)
-              d.p[c] = cheby_update<F>(alpha, d.p[c], beta * d.Mi[c], rv);
-            else
-              d.p[c] = cheby_update<F>(alpha, d.p[c], beta, rv);
+#pragma unroll 1
+      for (int g = y0; g < y0 + TH; g += 4) {
+        const long long c0 = cidx(d, x, g);
+        double wl[4], rl[4], pl[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          if (g + j < d.y_max) {
+            const long long c = c0 + j * d.S;
+            const double wv = smvp<F>(d, d.u, c);
+            const double rv = d.u0[c] - wv;
+            wl[j] = wv;
+            rl[j] = rv;
+            if (mode == 0) {
+              if (d.prec == PREC_JAC_DIAG)
+                pl[j] = (d.Mi[c] * rv) / theta;
+              else
+                pl[j] = rv / theta;
+            } else {
+              if (d.prec == PREC_JAC_DIAG)
+                pl[j] = cheby_update<F>(alpha, d.p[c], beta * d.Mi[c], rv);
+              else
+                pl[j] = cheby_update<F>(alpha, d.p[c], beta, rv);
+            }
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          if (g + j < d.y_max) {
+            const long long c = c0 + j * d.S;
+            d.w[c] = wl[j];
+            d.r[c] = rl[j];
+            d.p[c] = pl[j];
           }
         }
       }
@@ -604,13 +526,19 @@ template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock) k_cheby_calc_u(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
-#pragma unroll 4
-    for (int j = 0; j < TH; j++) {
-      const int y = y0 + j;
-      if (y < d.y_max) {
-        const long long c = cidx(d, x, y);
-        d.u[c] = d.u[c] + d.p[c];
-      }
+#pragma unroll 1
+    for (int g = y0; g < y0 + TH; g += 4) {
+      const long long c0 = cidx(d, x, g);
+      double uv[4], pv[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (g + j < d.y_max) {
+          uv[j] = d.u[c0 + j * d.S];
+          pv[j] = d.p[c0 + j * d.S];
+        }
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (g + j < d.y_max) d.u[c0 + j * d.S] = uv[j] + pv[j];
     }
   });
 }
@@ -630,9 +558,13 @@ __global__ void __launch_bounds__(kBlock)
       for (int ys = y0; ys < y0 + TH && ys < d.y_max; ys += 4) {
         double zl[4], rl[4];
         const long long c0 = cidx(d, x, ys);
+        double sv[4];
 #pragma unroll
-        for (int i = 0; i < 4; i++)
-          rl[i] = (ys + i < d.y_max) ? d.r[c0 + i * d.S] : 0.0;
+        for (int i = 0; i < 4; i++) {
+          const bool in = ys + i < d.y_max;
+          rl[i] = in ? d.r[c0 + i * d.S] : 0.0;
+          sv[i] = (in && mode != 0) ? d.sd[c0 + i * d.S] : 0.0;
+        }
         strip_solve<F>(d, c0, strip_rows(d, ys), rl, zl);
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -641,29 +573,36 @@ __global__ void __launch_bounds__(kBlock)
             if (mode == 0)
               d.sd[c] = zl[i] / theta;
             else
-              d.sd[c] = cheby_update<F>(alpha, d.sd[c], beta, zl[i]);
+              d.sd[c] = cheby_update<F>(alpha, sv[i], beta, zl[i]);
           }
         }
       }
     } else {
-#pragma unroll 4
-      for (int j = 0; j < TH; j++) {
-        const int y = y0 + j;
-        if (y < d.y_max) {
-          const long long c = cidx(d, x, y);
-          const double rv = d.r[c];
-          if (mode == 0) {
-            if (d.prec == PREC_JAC_DIAG)
-              d.sd[c] = rv * d.Mi[c] / theta;
-            else
-              d.sd[c] = rv / theta;
-          } else {
-            if (d.prec == PREC_JAC_DIAG)
-              d.sd[c] = cheby_update<F>(alpha, d.sd[c], beta * rv, d.Mi[c]);
-            else
-              d.sd[c] = cheby_update<F>(alpha, d.sd[c], beta, rv);
+#pragma unroll 1
+      for (int g = y0; g < y0 + TH; g += 4) {
+        const long long c0 = cidx(d, x, g);
+        double nv[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          if (g + j < d.y_max) {
+            const long long c = c0 + j * d.S;
+            const double rv = d.r[c];
+            if (mode == 0) {
+              if (d.prec == PREC_JAC_DIAG)
+                nv[j] = rv * d.Mi[c] / theta;
+              else
+                nv[j] = rv / theta;
+            } else {
+              if (d.prec == PREC_JAC_DIAG)
+                nv[j] = cheby_update<F>(alpha, d.sd[c], beta * rv, d.Mi[c]);
+              else
+                nv[j] = cheby_update<F>(alpha, d.sd[c], beta, rv);
+            }
           }
         }
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          if (g + j < d.y_max) d.sd[c0 + j * d.S] = nv[j];
       }
     }
   });
@@ -674,15 +613,24 @@ template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock) k_ppcg_update_r(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
-#pragma unroll 4
-    for (int j = 0; j < TH; j++) {
-      const int y = y0 + j;
-      if (y < d.y_max) {
-        const long long c = cidx(d, x, y);
-        d.u[c] = d.u[c] + d.sd[c];
-        const double result = smvp<F>(d, d.sd, c);
-        d.r[c] = d.r[c] - result;
-      }
+#pragma unroll 1
+    for (int g = y0; g < y0 + TH; g += 4) {
+      const long long c0 = cidx(d, x, g);
+      double uv[4], rv[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (g + j < d.y_max) {
+          const long long c = c0 + j * d.S;
+          uv[j] = d.u[c] + d.sd[c];
+          const double result = smvp<F>(d, d.sd, c);
+          rv[j] = d.r[c] - result;
+        }
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (g + j < d.y_max) {
+          d.u[c0 + j * d.S] = uv[j];
+          d.r[c0 + j * d.S] = rv[j];
+        }
     }
   });
 }
@@ -693,13 +641,16 @@ template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock) k_jacobi_copy_u(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
-#pragma unroll 4
-    for (int j = 0; j < TH; j++) {
-      const int y = y0 + j;
-      if (y < d.y_max) {
-        const long long c = cidx(d, x, y);
-        d.un[c] = d.u[c];
-      }
+#pragma unroll 1
+    for (int g = y0; g < y0 + TH; g += 4) {
+      const long long c0 = cidx(d, x, g);
+      double uv[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (g + j < d.y_max) uv[j] = d.u[c0 + j * d.S];
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (g + j < d.y_max) d.un[c0 + j * d.S] = uv[j];
     }
   });
 }
@@ -710,22 +661,28 @@ template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock) k_jacobi_solve(Dev d, Red red) {
   tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
     const long long S = d.S;
-#pragma unroll 4
-    for (int j = 0; j < TH; j++) {
-      const int y = y0 + j;
-      double v = 0.0;
-      if (xin && y < d.y_max) {
-        const long long c = cidx(d, x, y);
-        const double* un = d.un;
-        const double kxc = d.Kx[c], kxe = d.Kx[c + 1];
-        const double kyc = d.Ky[c], kyn = d.Ky[c + S];
-        const double u1 = (d.u0[c] + kxe * un[c + 1] + kxc * un[c - 1] +
-                           kyn * un[c + S] + kyc * un[c - S]) /
-                          (1.0 + (kxc + kxe) + (kyc + kyn));
-        d.u[c] = u1;
-        v = fabs(u1 - un[c]);
-      }
-      acc[0] = acc[0] + v;
+#pragma unroll 1
+    for (int g = y0; g < y0 + TH; g += 4) {
+      const long long c0 = cidx(d, x, g);
+      double uv[4], v[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (xin && g + j < d.y_max) {
+          const long long c = c0 + j * S;
+          const double* un = d.un;
+          const double kxc = d.Kx[c], kxe = d.Kx[c + 1];
+          const double kyc = d.Ky[c], kyn = d.Ky[c + S];
+          const double u1 = (d.u0[c] + kxe * un[c + 1] + kxc * un[c - 1] +
+                             kyn * un[c + S] + kyc * un[c - S]) /
+                            (1.0 + (kxc + kxe) + (kyc + kyn));
+          uv[j] = u1;
+          v[j] = fabs(u1 - un[c]);
+        }
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (xin && g + j < d.y_max) d.u[c0 + j * S] = uv[j];
+#pragma unroll
+      for (int j = 0; j < 4; j++) acc[0] = acc[0] + v[j];
     }
   });
 }
@@ -735,13 +692,16 @@ template <int TH, bool F>
 __global__ void __launch_bounds__(kBlock) k_finalise(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
-#pragma unroll 4
-    for (int j = 0; j < TH; j++) {
-      const int y = y0 + j;
-      if (y < d.y_max) {
-        const long long c = cidx(d, x, y);
-        d.energy1[c] = d.u[c] / d.density[c];
-      }
+#pragma unroll 1
+    for (int g = y0; g < y0 + TH; g += 4) {
+      const long long c0 = cidx(d, x, g);
+      double ev[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (g + j < d.y_max) ev[j] = d.u[c0 + j * d.S] / d.density[c0 + j * d.S];
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (g + j < d.y_max) d.energy1[c0 + j * d.S] = ev[j];
     }
   });
 }
@@ -933,6 +893,103 @@ void launch_update_halo(Chunk& c, int mask, int depth) {
   if (!mask || depth < 1) return;
   launch_2d(c, "update_halo", d.x_max + 2 * depth, d.y_max + 2 * depth,
             k_update_halo, d, mask, depth);
+}
+
+// ---------------------------------------------------------------------------
+// launchers for an explicit field set (batched problems)
+// ---------------------------------------------------------------------------
+
+Dev make_dev_tiling(Dev d) {
+  const int TH = reduction_rows(d.x_max, d.y_max);
+  d.th = TH;
+  d.xs = d.x_max + 2 * d.H;
+  d.ys = d.y_max + 2 * d.H;
+  d.block_top_check = (d.y_max % 4) != 0;
+  d.ntx = (d.x_max + kTileW - 1) / kTileW;
+  d.nsx = (d.ntx + kTilesPerSuper - 1) / kTilesPerSuper;
+  d.nty = (d.y_max + TH - 1) / TH;
+  d.ns = d.nsx * d.nty;
+  return d;
+}
+
+template <class... KArgs, class... Args>
+static void ctx_tile(const LaunchCtx& l, const Dev& d, const char* name,
+                     void (*kernel)(KArgs...), Args... args) {
+  const long long cap = (long long)l.num_sms * blocks_per_sm((const void*)kernel);
+  const int grid = (int)std::max<long long>(1, std::min<long long>(d.ns, cap));
+  kernel<<<grid, kBlock, 0, l.stream>>>(args...);
+  count_launch(name);
+  check_cuda(cudaGetLastError(), name);
+}
+
+template <class... KArgs, class... Args>
+static void ctx_2d(const LaunchCtx& l, const char* name, int nx, int ny,
+                   void (*kernel)(KArgs...), Args... args) {
+  if (nx <= 0 || ny <= 0) return;
+  kernel<<<dim3((nx + 31) / 32, (ny + 7) / 8), dim3(32, 8), 0, l.stream>>>(args...);
+  count_launch(name);
+  check_cuda(cudaGetLastError(), name);
+}
+
+#define CTX_DISPATCH(l, d, name, kern, ...)                       \
+  do {                                                            \
+    if ((d).th == 16) {                                           \
+      if ((l).fused)                                              \
+        ctx_tile(l, d, name, kern<16, true>, __VA_ARGS__);        \
+      else                                                        \
+        ctx_tile(l, d, name, kern<16, false>, __VA_ARGS__);       \
+    } else {                                                      \
+      if ((l).fused)                                              \
+        ctx_tile(l, d, name, kern<4, true>, __VA_ARGS__);         \
+      else                                                        \
+        ctx_tile(l, d, name, kern<4, false>, __VA_ARGS__);        \
+    }                                                             \
+  } while (0)
+
+void dev_volume(const LaunchCtx& l, const Dev& d, double vol) {
+  ctx_2d(l, "initialise_chunk_second", d.x_max + 2, d.y_max + 2, k_volume, d, vol);
+}
+void dev_init_common(const LaunchCtx& l, const Dev& d, int coef, double rx,
+                     double ry) {
+  ctx_2d(l, "tea_leaf_init_common", d.xs - 1, d.ys - 1, k_init_common, d, coef, rx, ry);
+}
+void dev_zero_boundary(const LaunchCtx& l, const Dev& d, const int* zb) {
+  ctx_2d(l, "tea_leaf_zero_boundary", d.xs, d.ys, k_zero_boundary, d, zb[0], zb[1],
+         zb[2], zb[3]);
+}
+void dev_init_diag(const LaunchCtx& l, const Dev& d, const Red& r) {
+  CTX_DISPATCH(l, d, "tea_leaf_init_diag", k_init_diag, d, r);
+}
+void dev_init_jac_diag(const LaunchCtx& l, const Dev& d) {
+  ctx_2d(l, "tea_leaf_init_jac_diag", d.xs, d.ys, k_init_jac_diag, d);
+}
+void dev_init_u(const LaunchCtx& l, const Dev& d, const double* energy) {
+  ctx_2d(l, "generate_chunk_init_u", d.x_max, d.y_max, k_init_u, d, energy);
+}
+void dev_calc_residual(const LaunchCtx& l, const Dev& d, const Red& r) {
+  CTX_DISPATCH(l, d, "tea_leaf_calc_residual", k_calc_residual, d, r);
+}
+void dev_dot(const LaunchCtx& l, const Dev& d, const Red& r, const double* a,
+             const double* b) {
+  CTX_DISPATCH(l, d, "tea_leaf_calc_2norm", k_dot, d, r, a, b);
+}
+void dev_block_init(const LaunchCtx& l, const Dev& d) {
+  ctx_2d(l, "tea_leaf_block_init", d.x_max, (d.y_max + 3) / 4, k_block_init, d,
+         l.fused ? 1 : 0);
+}
+void dev_update_halo(const LaunchCtx& l, const Dev& d, int mask, int depth) {
+  if (!mask || depth < 1) return;
+  ctx_2d(l, "update_halo", d.x_max + 2 * depth, d.y_max + 2 * depth, k_update_halo,
+         d, mask, depth);
+}
+void dev_cg_init_p(const LaunchCtx& l, const Dev& d, const Red& r) {
+  CTX_DISPATCH(l, d, "tea_leaf_cg_solve_init_p", k_cg_init_p, d, r);
+}
+void dev_finalise(const LaunchCtx& l, const Dev& d, const Red& r) {
+  CTX_DISPATCH(l, d, "tea_leaf_finalise", k_finalise, d, r);
+}
+void dev_field_summary(const LaunchCtx& l, const Dev& d, const Red& r) {
+  CTX_DISPATCH(l, d, "field_summary", k_field_summary, d, r);
 }
 
 // ---------------------------------------------------------------------------

@@ -85,3 +85,73 @@ def chebyshev_coefficients(eigmin, eigmax, n):
         betas.append(2.0 * rho_new / delta)
         rho_old = rho_new
     return alphas, betas, theta
+
+
+# ---------------------------------------------------------------------------
+# batched workloads: many independent problems of uneven size
+# ---------------------------------------------------------------------------
+
+BATCH_BACKGROUND = dict(density=100.0, energy=1e-4)
+
+
+def batch_problems(n, seed=0, side=(64, 1024), rects=(2, 6), extent=10.0):
+    """n seeded random problems on [0,extent]^2: x and y cell counts drawn
+    uniformly from `side`, each with 2-6 axis-aligned rectangles of density
+    log-uniform in [0.05, 200] and energy uniform in [1e-4, 25] painted over
+    the density-100, energy-1e-4 background."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        x = int(rng.integers(side[0], side[1] + 1))
+        y = int(rng.integers(side[0], side[1] + 1))
+        k = int(rng.integers(rects[0], rects[1] + 1))
+        states = []
+        for _ in range(k):
+            x0, x1 = sorted(float(v) for v in rng.uniform(0.0, extent, 2))
+            y0, y1 = sorted(float(v) for v in rng.uniform(0.0, extent, 2))
+            dens = float(np.exp(rng.uniform(np.log(0.05), np.log(200.0))))
+            en = float(rng.uniform(1e-4, 25.0))
+            states.append(dict(density=dens, energy=en, xmin=x0, xmax=x1, ymin=y0, ymax=y1))
+        out.append(dict(x=x, y=y, states=states))
+    return out
+
+
+def batch_deck(problem, steps=5, eps=1e-12, max_iters=5000, prec="jac_diag",
+               dt=0.004, arithmetic=None, extent=10.0):
+    """tea.in deck of one batched problem for a single-chunk CG run."""
+    lines = ["*tea", "state 1 density=%r energy=%r" % (BATCH_BACKGROUND["density"],
+                                                       BATCH_BACKGROUND["energy"])]
+    for k, s in enumerate(problem["states"]):
+        lines.append("state %d density=%r energy=%r geometry=rectangle xmin=%r xmax=%r "
+                     "ymin=%r ymax=%r" % (k + 2, s["density"], s["energy"], s["xmin"],
+                                          s["xmax"], s["ymin"], s["ymax"]))
+    lines += ["x_cells=%d" % problem["x"], "y_cells=%d" % problem["y"],
+              "xmin=0.0", "ymin=0.0", "xmax=%r" % extent, "ymax=%r" % extent,
+              "initial_timestep=%r" % dt, "end_step=%d" % steps,
+              "tl_max_iters=%d" % max_iters, "tl_use_cg", "tl_eps=%r" % eps,
+              "halo_depth=1", "summary_frequency=0"]
+    if prec != "none":
+        lines.append("tl_preconditioner_type=%s" % prec)
+    if arithmetic:
+        lines.append("tl_arithmetic %s" % arithmetic)
+    lines.append("*endtea")
+    return "\n".join(lines) + "\n"
+
+
+def paint(problem, extent=10.0):
+    """(density, energy) arrays (y, x) of a batched problem: a cell takes
+    the last state whose rectangle holds its centre."""
+    import numpy as np
+    x, y = problem["x"], problem["y"]
+    xc = (np.arange(x) + 0.5) * (extent / x)
+    yc = (np.arange(y) + 0.5) * (extent / y)
+    dens = np.full((y, x), BATCH_BACKGROUND["density"])
+    en = np.full((y, x), BATCH_BACKGROUND["energy"])
+    for s in problem["states"]:
+        mx = (xc >= s["xmin"]) & (xc < s["xmax"])
+        my = (yc >= s["ymin"]) & (yc < s["ymax"])
+        m = my[:, None] & mx[None, :]
+        dens[m] = s["density"]
+        en[m] = s["energy"]
+    return dens, en

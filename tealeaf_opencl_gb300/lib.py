@@ -44,6 +44,10 @@ EXTRA_SYMBOLS = [
     "tea_gb300_kernel_timer_read_name", "tea_gb300_fp64_rate",
     "tea_gb300_dot_noalloc", "tea_gb300_mixed_solve",
     "tea_gb300_driver_open", "tea_gb300_driver_step", "tea_gb300_driver_close",
+    "tea_gb300_batch_create", "tea_gb300_batch_set_fields", "tea_gb300_batch_run",
+    "tea_gb300_batch_summary", "tea_gb300_batch_iterations",
+    "tea_gb300_batch_read_field", "tea_gb300_batch_set_launch",
+    "tea_gb300_batch_get_launch", "tea_gb300_batch_autotune", "tea_gb300_batch_free",
 ]
 
 
@@ -68,6 +72,26 @@ class MixedInfo(C.Structure):
         ("initial_residual", C.c_double), ("final_residual", C.c_double),
         ("relative_residual", C.c_double),
     ]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [
+        ("steps", C.c_int), ("max_iterations", C.c_int), ("iterations", C.c_longlong),
+        ("cell_iterations", C.c_double), ("graph_launches", C.c_int),
+        ("kernel_launches", C.c_longlong), ("solve_ms", C.c_double),
+        ("total_ms", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class BatchLaunch(C.Structure):
+    _fields_ = [("blocks_per_sm", C.c_int), ("graph_iterations", C.c_int),
+                ("supertiles_per_unit", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class TeaError(RuntimeError):
@@ -146,6 +170,16 @@ def load(build=True):
         "tea_gb300_driver_open": (i, [C.c_char_p, C.c_char_p, i, i]),
         "tea_gb300_driver_step": (i, [C.POINTER(StepInfo)]),
         "tea_gb300_driver_close": (v, []),
+        "tea_gb300_batch_create": (i, [i, PI, PI, d, d, d, d, i, i]),
+        "tea_gb300_batch_set_fields": (i, [i, PD, PD]),
+        "tea_gb300_batch_run": (i, [i, d, d, i, C.POINTER(BatchStats)]),
+        "tea_gb300_batch_summary": (i, [i, PD]),
+        "tea_gb300_batch_iterations": (i, [i, PI, i]),
+        "tea_gb300_batch_read_field": (i, [i, i, PD]),
+        "tea_gb300_batch_set_launch": (i, [C.POINTER(BatchLaunch)]),
+        "tea_gb300_batch_get_launch": (i, [C.POINTER(BatchLaunch)]),
+        "tea_gb300_batch_autotune": (i, [C.POINTER(BatchLaunch)]),
+        "tea_gb300_batch_free": (v, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -391,3 +425,84 @@ def run_deck(deck_text, mode=DRIVER_PER_CALL, max_iters_cap=0, log_path=None):
     finally:
         drv.close()
     return steps
+
+
+class Batch:
+    """Many independent single-chunk CG problems solved together on the GPU
+    (tea_gb300_batch_* in include/tealeaf_gb300.h).  sizes: list of
+    (x_cells, y_cells)."""
+
+    def __init__(self, sizes, prec="jac_diag", coefficient=1,
+                 extent=(0.0, 10.0, 0.0, 10.0)):
+        L = load()
+        self.sizes = [(int(x), int(y)) for x, y in sizes]
+        xs = np.array([x for x, _ in self.sizes], dtype=np.int32)
+        ys = np.array([y for _, y in self.sizes], dtype=np.int32)
+        self.steps = 0
+        if L.tea_gb300_batch_create(len(self.sizes), _pi(xs), _pi(ys), *map(float, extent),
+                                    PREC[prec] if isinstance(prec, str) else int(prec),
+                                    int(coefficient)) != 0:
+            check()
+            raise TeaError("batch_create failed")
+
+    def set_fields(self, i, density, energy):
+        x, y = self.sizes[i]
+        d = np.ascontiguousarray(density, dtype=np.float64)
+        e = np.ascontiguousarray(energy, dtype=np.float64)
+        assert d.shape == (y, x) and e.shape == (y, x)
+        if load().tea_gb300_batch_set_fields(i, _pd(d), _pd(e)) != 0:
+            check()
+            raise TeaError("batch_set_fields failed")
+
+    def run(self, steps, dt, eps, max_iters):
+        st = BatchStats()
+        if load().tea_gb300_batch_run(int(steps), float(dt), float(eps), int(max_iters),
+                                      C.byref(st)) != 0:
+            check()
+            raise TeaError("batch_run failed")
+        self.steps = int(steps)
+        return st
+
+    def summary(self, i):
+        out = np.zeros(4)
+        if load().tea_gb300_batch_summary(i, _pd(out)) != 0:
+            check()
+            raise TeaError("batch_summary failed")
+        return tuple(out)
+
+    def iterations(self, i):
+        out = np.zeros(self.steps, dtype=np.int32)
+        if load().tea_gb300_batch_iterations(i, _pi(out), self.steps) != 0:
+            check()
+            raise TeaError("batch_iterations failed")
+        return [int(v) for v in out]
+
+    def read(self, i, name):
+        x, y = self.sizes[i]
+        out = np.zeros((y, x))
+        if load().tea_gb300_batch_read_field(i, FIELD[name], _pd(out)) != 0:
+            check()
+            raise TeaError("batch_read_field failed")
+        return out
+
+    def launch(self):
+        l = BatchLaunch()
+        if load().tea_gb300_batch_get_launch(C.byref(l)) != 0:
+            check()
+        return l.as_dict()
+
+    def set_launch(self, blocks_per_sm, graph_iterations=16, supertiles_per_unit=1):
+        l = BatchLaunch(int(blocks_per_sm), int(graph_iterations), int(supertiles_per_unit))
+        if load().tea_gb300_batch_set_launch(C.byref(l)) != 0:
+            check()
+            raise TeaError("batch_set_launch failed")
+
+    def autotune(self):
+        l = BatchLaunch()
+        if load().tea_gb300_batch_autotune(C.byref(l)) != 0:
+            check()
+            raise TeaError("batch_autotune failed")
+        return l.as_dict()
+
+    def free(self):
+        load().tea_gb300_batch_free()
