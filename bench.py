@@ -532,6 +532,89 @@ def run_batch(args):
     return out
 
 
+def run_adjoint(args):
+    """Gradient of 0.5*||u_T - u_obs||^2 w.r.t. per-cell log-density through
+    args.steps implicit CG timesteps (jac_diag, FP64) on the five-state
+    problem at args.cells^2, with u_obs from a forward run whose density is
+    perturbed by a seeded smooth log-normal field.  Times the forward pass
+    (with checkpoints every 4 steps) and the adjoint pass, then checks the
+    gradient against central finite differences on args.directions random
+    directions, and against the FP64 torch-autograd reference gradient on a
+    small problem (args.ref_cells^2)."""
+    import numpy as np
+    import torch
+    from tealeaf_opencl_gb300 import adjoint, decks, lib
+    from tests import adjoint_reference as ref
+    L = lib.load()
+    n, steps, dt = args.cells, args.steps, 0.004
+    deck = decks.five_state_deck(n, solver="cg", prec="jac_diag", steps=1,
+                                 summary_frequency=0)
+    drv = lib.Driver(deck)
+    dens = lib.read_field("density")
+    en = lib.read_field("energy1")
+    drv.close()
+    L.tea_gb300_finalise()
+    L.tea_gb300_set_arithmetic(1)
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+    adj = lib.Adjoint(n, n)
+    d, e = dev(dens), dev(en)
+    cfg = adj.config(steps, dt, args.eps, 20000, 4)
+    u_obs = torch.empty_like(d)
+    adj.forward(dev(dens * np.exp(ref.smooth_field((n, n), 2024, sigma=0.3, corr=16.0))), e,
+                u_final=u_obs, cfg=cfg)
+    loss, fst = adj.forward(d, e, u_obs, cfg=cfg)
+    g = torch.empty_like(d)
+    bst = adj.backward(g)
+    out = {"mode": "adjoint", "cells": n * n, "steps": steps, "dt": dt, "eps": args.eps,
+           "checkpoint_every": 4, "dtype": "f64", "loss": loss,
+           "forward_ms": fst.forward_ms, "backward_ms": bst.backward_ms,
+           "backward_over_forward": bst.backward_ms / fst.forward_ms,
+           "iterations": {"forward": fst.forward_iterations,
+                          "recompute": bst.recompute_iterations,
+                          "adjoint": bst.adjoint_iterations},
+           "checkpoints": bst.checkpoints,
+           "grad_norm": float(g.norm())}
+    theta = torch.log(d)
+    gen = torch.Generator(device="cuda").manual_seed(args.seed)
+    h = args.fd_step
+    errs = []
+    t0 = time.perf_counter()
+    for _ in range(args.directions):
+        v = torch.randn(theta.shape, dtype=torch.float64, device="cuda", generator=gen)
+        lp = adjoint.time_stepped_loss(theta + h * v, e, u_obs, adj, cfg)
+        lm = adjoint.time_stepped_loss(theta - h * v, e, u_obs, adj, cfg)
+        fd = float((lp - lm) / (2 * h))
+        gv = float((g * v).sum())
+        errs.append({"fd": fd, "adjoint": gv, "rel_err": abs(fd - gv) / abs(fd)})
+    out["finite_differences"] = {"directions": args.directions, "step": h,
+                                 "max_rel_err": max(x["rel_err"] for x in errs),
+                                 "seconds": time.perf_counter() - t0, "each": errs}
+    adj.free()
+    # the FP64 reference gradient (dense direct solves, torch autograd)
+    m = args.ref_cells
+    deck = decks.five_state_deck(m, solver="cg", prec="jac_diag", steps=1, summary_frequency=0)
+    drv = lib.Driver(deck)
+    dens_s, en_s = lib.read_field("density"), lib.read_field("energy1")
+    drv.close()
+    L.tea_gb300_finalise()
+    L.tea_gb300_set_arithmetic(1)
+    adj = lib.Adjoint(m, m)
+    cfg_s = adj.config(steps, dt, 1e-15, 20000, 4)
+    uo = torch.empty((m, m), dtype=torch.float64, device="cuda")
+    adj.forward(dev(dens_s * np.exp(ref.smooth_field((m, m), 7, sigma=0.3, corr=4.0))),
+                dev(en_s), u_final=uo, cfg=cfg_s)
+    loss_s, _ = adj.forward(dev(dens_s), dev(en_s), uo, cfg=cfg_s)
+    gs = torch.empty_like(uo)
+    adj.backward(gs)
+    adj.free()
+    loss_r, g_r = ref.loss_and_gradient(dens_s, en_s, uo.cpu().numpy(), steps, dt)
+    out["fp64_reference"] = {
+        "cells": m * m, "eps": 1e-15,
+        "loss_rel_err": abs(loss_s - loss_r) / abs(loss_r),
+        "grad_max_abs_err_over_max": float(np.abs(gs.cpu().numpy() - g_r).max() / np.abs(g_r).max())}
+    return out
+
+
 def cpu_sample(name, steps_timed, cap):
     """Oracle on the same deck: one warm-up step, then steps_timed steps,
     every step capped at `cap` outer iterations; returns (value, detail)."""
@@ -592,7 +675,8 @@ def main():
     ap.add_argument("--cap", type=int, default=0,
                     help="limit solver iterations per GPU step (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="run", choices=["run", "kernels", "mixed", "batch"],
+    ap.add_argument("--mode", default="run",
+                    choices=["run", "kernels", "mixed", "batch", "adjoint"],
                     help="kernels: time each hot entry point on the workload's grid; "
                          "mixed: FP64 vs FP32-inner/FP64-refined CG to 1e-10")
     ap.add_argument("--cells", type=int, default=4096, help="grid side for --mode mixed")
@@ -601,6 +685,13 @@ def main():
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--problems", type=int, default=512, help="--mode batch: problem count")
     ap.add_argument("--seed", type=int, default=0, help="--mode batch: problem seed")
+    ap.add_argument("--directions", type=int, default=16,
+                    help="--mode adjoint: finite-difference directions")
+    ap.add_argument("--fd-step", type=float, default=1e-6,
+                    help="--mode adjoint: central-difference step in log-density")
+    ap.add_argument("--eps", type=float, default=1e-12, help="--mode adjoint: CG tolerance")
+    ap.add_argument("--ref-cells", type=int, default=32,
+                    help="--mode adjoint: side of the FP64 reference-gradient problem")
     ap.add_argument("--sequential", type=int, default=32,
                     help="--mode batch: problems also run one by one for comparison")
     args = ap.parse_args()
@@ -626,6 +717,9 @@ def main():
         return
     if args.mode == "batch":
         print(json.dumps(run_batch(args)))
+        return
+    if args.mode == "adjoint":
+        print(json.dumps(run_adjoint(args)))
         return
 
     dist = Dist()

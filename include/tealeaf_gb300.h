@@ -405,6 +405,59 @@ int tea_gb300_batch_autotune(tea_gb300_batch_launch* best);
 /* Releases the batch. */
 void tea_gb300_batch_free(void);
 
+/* ---- adjoint of the time-stepped solve (no counterpart in the reference) ----
+ *
+ * The forward model is `steps` TeaLeaf timesteps on one chunk with CG, all
+ * faces external and zeroed boundary faces (tea_solve.f90:37-420): each step
+ * u0 = energy*density, solve (I + dt L_K) u = u0 to eps*||r0||, energy =
+ * u/density.  Its iteration counts and its final u are bit-identical to the
+ * single-chunk driver's.  The loss is 0.5*||u_T - u_obs||^2.  The adjoint
+ * gives d loss / d log(density) per cell: one CG solve with the same
+ * (symmetric) operator per step, backwards, and one fused kernel per step that
+ * turns the face-coefficient gradient -(mu_a - mu_b)(u_a - u_b) into the
+ * per-cell log-density gradient.  Forward states are checkpointed every
+ * `checkpoint_every` steps; the steps in between are recomputed.  One adjoint
+ * object exists per process, with its own stream.  Field arguments are DEVICE
+ * pointers to x_cells*y_cells doubles, x fastest. */
+
+typedef struct {
+  int steps;             /* timesteps */
+  double dt;             /* timestep length */
+  double eps;            /* relative CG tolerance of every solve */
+  int max_iters;         /* CG iteration limit of every solve */
+  int checkpoint_every;  /* steps between stored states (>= 1) */
+} tea_gb300_adjoint_config;
+
+typedef struct {
+  long long forward_iterations;    /* CG iterations of the forward pass */
+  long long recompute_iterations;  /* of the recomputed steps */
+  long long adjoint_iterations;    /* of the adjoint solves */
+  int checkpoints;                 /* states kept by the forward pass */
+  double forward_ms;               /* GPU time of the last forward call */
+  double backward_ms;              /* GPU time of the last backward call */
+} tea_gb300_adjoint_stats;
+
+/* Sets up an x_cells by y_cells problem on [xmin,xmax] x [ymin,ymax] with
+ * the given coefficient (TEA_COEF_*) and preconditioner (TEA_PREC_NONE or
+ * TEA_PREC_JAC_DIAG), in the arithmetic form set by
+ * tea_gb300_set_arithmetic.  Replaces any earlier adjoint object. */
+int tea_gb300_adjoint_create(int x_cells, int y_cells, double xmin, double xmax,
+                             double ymin, double ymax, int coefficient,
+                             int preconditioner);
+/* Runs the forward model from density and energy0.  If u_obs is not NULL,
+ * *loss gets 0.5*||u_T - u_obs||^2 and the pass is kept for
+ * tea_gb300_adjoint_backward.  u_final (may be NULL) gets u_T. */
+int tea_gb300_adjoint_forward(const double* density, const double* energy0,
+                              const double* u_obs,
+                              const tea_gb300_adjoint_config* config,
+                              double* loss, double* u_final,
+                              tea_gb300_adjoint_stats* stats);
+/* d loss / d log(density) of the last forward pass into grad_log_density. */
+int tea_gb300_adjoint_backward(double* grad_log_density,
+                               tea_gb300_adjoint_stats* stats);
+/* Releases the adjoint object. */
+void tea_gb300_adjoint_free(void);
+
 #ifdef __cplusplus
 }
 #endif

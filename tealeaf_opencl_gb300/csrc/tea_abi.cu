@@ -30,6 +30,7 @@ Chunk& chunk() { return g_chunk; }
 
 static int g_abort_on_error = 1;
 static int g_err_code = 0;
+static long long g_err_count = 0;  // errors recorded since load
 static std::string g_err_msg;
 static long long g_launches = 0;
 
@@ -39,6 +40,7 @@ void fail(int code, const char* fmt, ...) {
   va_start(ap, fmt);
   vsnprintf(buf, sizeof(buf), fmt, ap);
   va_end(ap);
+  g_err_count++;
   if (g_err_code == 0) {
     g_err_code = code;
     g_err_msg = buf;
@@ -51,6 +53,7 @@ void fail(int code, const char* fmt, ...) {
 }
 
 int error_code() { return g_err_code; }
+long long error_count() { return g_err_count; }
 
 bool check_cuda(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return true;

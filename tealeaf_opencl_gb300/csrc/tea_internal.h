@@ -125,6 +125,7 @@ Chunk& chunk();
 // error handling (tea_abi.cu)
 void fail(int code, const char* fmt, ...);
 int error_code();
+long long error_count();  // errors recorded so far (never reset)
 bool check_cuda(cudaError_t e, const char* what);
 void count_launch(const char* name);
 void count_launches(long long n);  // n kernels run from a graph replay
@@ -188,6 +189,10 @@ void dev_dot(const LaunchCtx& l, const Dev& d, const Red& r, const double* a,
 void dev_block_init(const LaunchCtx& l, const Dev& d);
 void dev_update_halo(const LaunchCtx& l, const Dev& d, int mask, int depth);
 void dev_cg_init_p(const LaunchCtx& l, const Dev& d, const Red& r);
+// one iteration of the device-resident CG loop (loop scalars in *st; the
+// kernels return at once after it has stopped)
+void dev_cg_iteration(const LaunchCtx& l, const Dev& d, const Red& r, ResState* st,
+                      unsigned int* counter);
 void dev_finalise(const LaunchCtx& l, const Dev& d, const Red& r);
 void dev_field_summary(const LaunchCtx& l, const Dev& d, const Red& r);
 // device-resident CG loop (tea_kernels.cu)

@@ -985,6 +985,12 @@ void dev_update_halo(const LaunchCtx& l, const Dev& d, int mask, int depth) {
 void dev_cg_init_p(const LaunchCtx& l, const Dev& d, const Red& r) {
   CTX_DISPATCH(l, d, "tea_leaf_cg_solve_init_p", k_cg_init_p, d, r);
 }
+void dev_cg_iteration(const LaunchCtx& l, const Dev& d, const Red& r, ResState* st,
+                      unsigned int* counter) {
+  CTX_DISPATCH(l, d, "tea_leaf_cg_solve_calc_w", k_cg_calc_w, d, r, st);
+  CTX_DISPATCH(l, d, "tea_leaf_cg_solve_calc_ur", k_cg_calc_ur, d, r, 0.0, st);
+  CTX_DISPATCH(l, d, "tea_leaf_cg_solve_calc_p", k_cg_calc_p, d, r, 0.0, st, counter);
+}
 void dev_finalise(const LaunchCtx& l, const Dev& d, const Red& r) {
   CTX_DISPATCH(l, d, "tea_leaf_finalise", k_finalise, d, r);
 }

@@ -48,6 +48,8 @@ EXTRA_SYMBOLS = [
     "tea_gb300_batch_summary", "tea_gb300_batch_iterations",
     "tea_gb300_batch_read_field", "tea_gb300_batch_set_launch",
     "tea_gb300_batch_get_launch", "tea_gb300_batch_autotune", "tea_gb300_batch_free",
+    "tea_gb300_adjoint_create", "tea_gb300_adjoint_forward", "tea_gb300_adjoint_backward",
+    "tea_gb300_adjoint_free",
 ]
 
 
@@ -89,6 +91,22 @@ class BatchStats(C.Structure):
 class BatchLaunch(C.Structure):
     _fields_ = [("blocks_per_sm", C.c_int), ("graph_iterations", C.c_int),
                 ("supertiles_per_unit", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class AdjointConfig(C.Structure):
+    _fields_ = [("steps", C.c_int), ("dt", C.c_double), ("eps", C.c_double),
+                ("max_iters", C.c_int), ("checkpoint_every", C.c_int)]
+
+
+class AdjointStats(C.Structure):
+    _fields_ = [
+        ("forward_iterations", C.c_longlong), ("recompute_iterations", C.c_longlong),
+        ("adjoint_iterations", C.c_longlong), ("checkpoints", C.c_int),
+        ("forward_ms", C.c_double), ("backward_ms", C.c_double),
+    ]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -180,6 +198,12 @@ def load(build=True):
         "tea_gb300_batch_get_launch": (i, [C.POINTER(BatchLaunch)]),
         "tea_gb300_batch_autotune": (i, [C.POINTER(BatchLaunch)]),
         "tea_gb300_batch_free": (v, []),
+        "tea_gb300_adjoint_create": (i, [i, i, d, d, d, d, i, i]),
+        "tea_gb300_adjoint_forward": (i, [C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.POINTER(AdjointConfig), PD, C.c_void_p,
+                                          C.POINTER(AdjointStats)]),
+        "tea_gb300_adjoint_backward": (i, [C.c_void_p, C.POINTER(AdjointStats)]),
+        "tea_gb300_adjoint_free": (v, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -506,3 +530,55 @@ class Batch:
 
     def free(self):
         load().tea_gb300_batch_free()
+
+
+def _devptr(t):
+    """Device address of a CUDA tensor (or an int address), or None."""
+    if t is None:
+        return None
+    return C.c_void_p(t if isinstance(t, int) else t.data_ptr())
+
+
+class Adjoint:
+    """The time-stepped solve and its adjoint w.r.t. log-density
+    (tea_gb300_adjoint_* in include/tealeaf_gb300.h).  Field arguments are
+    contiguous float64 CUDA tensors of shape (y_cells, x_cells)."""
+
+    def __init__(self, x_cells, y_cells, coefficient=1, prec="jac_diag",
+                 extent=(0.0, 10.0, 0.0, 10.0)):
+        self.shape = (int(y_cells), int(x_cells))
+        if load().tea_gb300_adjoint_create(int(x_cells), int(y_cells), *map(float, extent),
+                                           int(coefficient),
+                                           PREC[prec] if isinstance(prec, str) else int(prec)) != 0:
+            check()
+            raise TeaError("adjoint_create failed")
+
+    @staticmethod
+    def config(steps, dt=0.004, eps=1e-12, max_iters=10000, checkpoint_every=4):
+        return AdjointConfig(int(steps), float(dt), float(eps), int(max_iters),
+                             int(checkpoint_every))
+
+    def forward(self, density, energy0, u_obs=None, u_final=None, cfg=None):
+        """Runs the forward model; returns (loss or None, AdjointStats)."""
+        for t in (density, energy0, u_obs, u_final):
+            if t is not None and not isinstance(t, int):
+                assert t.is_cuda and t.is_contiguous() and tuple(t.shape) == self.shape
+        loss = C.c_double()
+        st = AdjointStats()
+        if load().tea_gb300_adjoint_forward(_devptr(density), _devptr(energy0), _devptr(u_obs),
+                                            C.byref(cfg), C.byref(loss), _devptr(u_final),
+                                            C.byref(st)) != 0:
+            check()
+            raise TeaError("adjoint_forward failed")
+        return (loss.value if u_obs is not None else None), st
+
+    def backward(self, grad_out):
+        """d loss / d log(density) of the last forward pass into grad_out."""
+        st = AdjointStats()
+        if load().tea_gb300_adjoint_backward(_devptr(grad_out), C.byref(st)) != 0:
+            check()
+            raise TeaError("adjoint_backward failed")
+        return st
+
+    def free(self):
+        load().tea_gb300_adjoint_free()
