@@ -62,6 +62,15 @@ struct MixChunk {
 
 static MixChunk g_mix;
 
+// Rows per load group of the FP32 iteration kernels, and their minimum
+// resident blocks per SM.  Measured at 4096^2 (ms per inner iteration):
+// groups of 1/2/4/8 rows at 8 blocks/SM (32 registers) 0.229/0.240/0.252/-,
+// groups of 4 or 8 rows without the bound 0.277/0.303.  Occupancy is what
+// keeps these HBM-bound kernels fed.
+template <int TH>
+constexpr int kGroup = 1;
+constexpr int kMixMinBlocks = 8;
+
 __device__ __forceinline__ long long cidx32(const Dev& d, const MixDev& m, int x,
                                             int y) {
   return (long long)(y + d.H) * m.S + (x + d.H);
@@ -120,24 +129,33 @@ __global__ void __launch_bounds__(kBlock)
     k_mix_residual(Dev d, MixDev m, Red red) {
   tile_driver<TH, 2>(d, red, [&](int x, int y0, bool xin, double* acc) {
     float hi = 0.0f, lo = 0.0f;
-#pragma unroll 2
-    for (int j = 0; j < TH; j++) {
-      const int y = y0 + j;
-      double r64 = 0.0;
-      float r32 = 0.0f, z = 0.0f;
-      if (xin && y < d.y_max) {
-        const long long c = cidx(d, x, y);
-        const long long c3 = cidx32(d, m, x, y);
-        r64 = d.u0[c] - smvp<true>(d, d.u, c);
-        d.r[c] = r64;
-        r32 = (float)r64;
-        z = m.Mi[c3] * r32;
-        m.r[c3] = r32;
-        m.p[c3] = z;
-        m.d[c3] = 0.0f;
+#pragma unroll 1
+    for (int g = y0; g < y0 + TH; g += 4) {
+      double r64[4];
+      float r32[4], z[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        r64[j] = 0.0;
+        r32[j] = z[j] = 0.0f;
+        if (xin && g + j < d.y_max) {
+          const long long c = cidx(d, x, g + j);
+          r64[j] = d.u0[c] - smvp<true>(d, d.u, c);
+          r32[j] = (float)r64[j];
+          z[j] = m.Mi[cidx32(d, m, x, g + j)] * r32[j];
+        }
       }
-      acc[0] = __fma_rn(r64, r64, acc[0]);
-      acc_pair(hi, lo, r32, z);
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        if (xin && g + j < d.y_max) {
+          const long long c3 = cidx32(d, m, x, g + j);
+          d.r[cidx(d, x, g + j)] = r64[j];
+          m.r[c3] = r32[j];
+          m.p[c3] = z[j];
+          m.d[c3] = 0.0f;
+        }
+        acc[0] = __fma_rn(r64[j], r64[j], acc[0]);
+        acc_pair(hi, lo, r32[j], z[j]);
+      }
     }
     acc[1] = pair_value(hi, lo);
   });
@@ -145,22 +163,29 @@ __global__ void __launch_bounds__(kBlock)
 
 // w = A p, sum p.w
 template <int TH>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, kMixMinBlocks)
     k_mix_calc_w(Dev d, MixDev m, Red red, MixState* st) {
   if (*(volatile int*)&st->stop) return;
   const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
     float hi = 0.0f, lo = 0.0f;
-#pragma unroll 4
-    for (int j = 0; j < TH; j++) {
-      const int y = y0 + j;
-      float pv = 0.0f, wv = 0.0f;
-      if (xin && y < d.y_max) {
-        const long long c3 = cidx32(d, m, x, y);
-        wv = smvp32(m, m.p, c3);
-        m.w[c3] = wv;
-        pv = m.p[c3];
+    constexpr int GR = kGroup<TH>;
+#pragma unroll 1
+    for (int g = y0; g < y0 + TH; g += GR) {
+      float pv[GR], wv[GR];
+#pragma unroll
+      for (int j = 0; j < GR; j++) {
+        pv[j] = wv[j] = 0.0f;
+        if (xin && g + j < d.y_max) {
+          const long long c3 = cidx32(d, m, x, g + j);
+          wv[j] = smvp32(m, m.p, c3);
+          pv[j] = m.p[c3];
+        }
       }
-      acc_pair(hi, lo, pv, wv);
+#pragma unroll
+      for (int j = 0; j < GR; j++) {
+        if (xin && g + j < d.y_max) m.w[cidx32(d, m, x, g + j)] = wv[j];
+        acc_pair(hi, lo, pv[j], wv[j]);
+      }
     }
     acc[0] = pair_value(hi, lo);
   });
@@ -170,25 +195,36 @@ __global__ void __launch_bounds__(kBlock)
 // alpha = rro/pw; d += alpha p; r -= alpha w; z = Mi r; sum r.z; the last
 // block takes the CG scalar step and the inner exit test
 template <int TH>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, kMixMinBlocks)
     k_mix_calc_ur(Dev d, MixDev m, Red red, MixState* st) {
   if (*(volatile int*)&st->stop) return;
   const double alpha = st->rro / st->pw;
   const float af = (float)alpha;
   const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
     float hi = 0.0f, lo = 0.0f;
-#pragma unroll 4
-    for (int j = 0; j < TH; j++) {
-      const int y = y0 + j;
-      float rv = 0.0f, zv = 0.0f;
-      if (xin && y < d.y_max) {
-        const long long c3 = cidx32(d, m, x, y);
-        m.d[c3] = __fmaf_rn(af, m.p[c3], m.d[c3]);
-        rv = __fmaf_rn(-af, m.w[c3], m.r[c3]);
-        m.r[c3] = rv;
-        zv = m.Mi[c3] * rv;
+    constexpr int GR = kGroup<TH>;
+#pragma unroll 1
+    for (int g = y0; g < y0 + TH; g += GR) {
+      float dv[GR], rv[GR], zv[GR];
+#pragma unroll
+      for (int j = 0; j < GR; j++) {
+        dv[j] = rv[j] = zv[j] = 0.0f;
+        if (xin && g + j < d.y_max) {
+          const long long c3 = cidx32(d, m, x, g + j);
+          dv[j] = __fmaf_rn(af, m.p[c3], m.d[c3]);
+          rv[j] = __fmaf_rn(-af, m.w[c3], m.r[c3]);
+          zv[j] = m.Mi[c3] * rv[j];
+        }
       }
-      acc_pair(hi, lo, rv, zv);
+#pragma unroll
+      for (int j = 0; j < GR; j++) {
+        if (xin && g + j < d.y_max) {
+          const long long c3 = cidx32(d, m, x, g + j);
+          m.d[c3] = dv[j];
+          m.r[c3] = rv[j];
+        }
+        acc_pair(hi, lo, rv[j], zv[j]);
+      }
     }
     acc[0] = pair_value(hi, lo);
   });
@@ -210,20 +246,23 @@ __global__ void __launch_bounds__(kBlock)
 
 // p = Mi r + beta p
 template <int TH>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, kMixMinBlocks)
     k_mix_calc_p(Dev d, MixDev m, Red red, MixState* st, unsigned int* counter) {
   if (!*(volatile int*)&st->p_pending) return;
   const float bf = (float)st->beta;
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
-#pragma unroll 4
+    float pv[TH];
+#pragma unroll
     for (int j = 0; j < TH; j++) {
-      const int y = y0 + j;
-      if (y < d.y_max) {
-        const long long c3 = cidx32(d, m, x, y);
-        m.p[c3] = __fmaf_rn(bf, m.p[c3], m.Mi[c3] * m.r[c3]);
+      if (y0 + j < d.y_max) {
+        const long long c3 = cidx32(d, m, x, y0 + j);
+        pv[j] = __fmaf_rn(bf, m.p[c3], m.Mi[c3] * m.r[c3]);
       }
     }
+#pragma unroll
+    for (int j = 0; j < TH; j++)
+      if (y0 + j < d.y_max) m.p[cidx32(d, m, x, y0 + j)] = pv[j];
   });
   if (last_block(counter) && threadIdx.x == 0) {
     st->p_pending = 0;
@@ -236,13 +275,16 @@ template <int TH>
 __global__ void __launch_bounds__(kBlock) k_mix_update_u(Dev d, MixDev m, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
-#pragma unroll 4
-    for (int j = 0; j < TH; j++) {
-      const int y = y0 + j;
-      if (y < d.y_max) {
-        const long long c = cidx(d, x, y);
-        d.u[c] = d.u[c] + (double)m.d[cidx32(d, m, x, y)];
-      }
+#pragma unroll 1
+    for (int g = y0; g < y0 + TH; g += 4) {
+      double uv[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (g + j < d.y_max)
+          uv[j] = d.u[cidx(d, x, g + j)] + (double)m.d[cidx32(d, m, x, g + j)];
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (g + j < d.y_max) d.u[cidx(d, x, g + j)] = uv[j];
     }
   });
 }
