@@ -412,12 +412,16 @@ def run_mixed(args):
     out = {"mode": "mixed", "cells": cells * cells, "steps": args.steps,
            "lognormal": bool(args.lognormal), "tol": 1e-10}
     ncell = cells * cells
+    out["mixed_inner_solver"] = args.mixed_solver
     for name, extra, mode in (("fp64", "tl_exit_true_residual", lib.DRIVER_RESIDENT),
                               ("mixed", "tl_mixed_precision\ntl_mixed_inner_eps 1e-5",
                                lib.DRIVER_PER_CALL)):
-        deck = decks.five_state_deck(cells, solver="cg", prec="jac_diag",
+        solver = args.mixed_solver if name == "mixed" else "cg"
+        deck = decks.five_state_deck(cells, solver=solver, prec="jac_diag",
                                      steps=args.steps, eps=1e-10, max_iters=100000,
-                                     summary_frequency=0, check_result=True, extra=extra)
+                                     summary_frequency=0, check_result=True, extra=extra,
+                                     inner_steps=args.inner_steps if solver == "ppcg" else None,
+                                     presteps=args.presteps if solver == "ppcg" else None)
         drv = lib.Driver(deck, mode=mode)
         if factor is not None:
             lib.write_field("density", lib.read_field("density") * factor)
@@ -432,6 +436,7 @@ def run_mixed(args):
         last = infos[-1]
         out[name] = {"seconds": sum(times), "step_seconds": times,
                      "iterations": [i.iterations for i in infos],
+                     "ppcg_inner_steps": [i.inner_iterations for i in infos],
                      "corrections": [i.outer_corrections for i in infos],
                      "relative_residual": [i.relative_residual if name == "mixed"
                                            else i.exact_error for i in infos],
@@ -680,6 +685,12 @@ def main():
                     help="kernels: time each hot entry point on the workload's grid; "
                          "mixed: FP64 vs FP32-inner/FP64-refined CG to 1e-10")
     ap.add_argument("--cells", type=int, default=4096, help="grid side for --mode mixed")
+    ap.add_argument("--mixed-solver", default="cg", choices=["cg", "ppcg"],
+                    help="--mode mixed: FP32 inner solver")
+    ap.add_argument("--presteps", type=int, default=25,
+                    help="--mode mixed --mixed-solver ppcg: CG presteps")
+    ap.add_argument("--inner-steps", type=int, default=10,
+                    help="--mode mixed --mixed-solver ppcg: Chebyshev steps per iteration")
     ap.add_argument("--lognormal", action="store_true",
                     help="--mode mixed: density times a seeded log-normal field")
     ap.add_argument("--reps", type=int, default=20)

@@ -296,9 +296,21 @@ typedef struct {
   double initial_residual;       /* ||u0 - A u||_2 at entry */
   double final_residual;         /* ||u0 - A u||_2 at return, FP64 */
   double relative_residual;      /* their ratio */
+  long long ppcg_inner_steps;    /* FP32 Chebyshev steps (PPCG inner solver) */
 } tea_gb300_mixed_info;
 int tea_gb300_mixed_solve(double tol, double inner_tol, int max_outer,
                           int max_inner, tea_gb300_mixed_info* info);
+/* The same solve with FP32 PPCG as the inner solver, as the driver's PPCG
+ * (tea_solve.f90:147-332, :422-475) in FP32 with diagonal Jacobi: the first
+ * correction starts with up to `presteps` CG iterations, whose alphas and
+ * betas give the eigenvalue range (x0.95, x1.05) and the Chebyshev
+ * coefficients of `inner_steps` inner steps, and continues, like every
+ * later correction, with PPCG iterations.  inner_iterations counts CG and
+ * PPCG iterations; ppcg_inner_steps the Chebyshev steps.  If the eigenvalue
+ * estimate fails the solve stays CG. */
+int tea_gb300_mixed_solve_ppcg(double tol, double inner_tol, int max_outer,
+                               int max_inner, int presteps, int inner_steps,
+                               tea_gb300_mixed_info* info);
 
 /* Waits for all work queued on the library's stream. */
 int tea_gb300_synchronize(void);

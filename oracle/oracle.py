@@ -50,7 +50,7 @@ class MixedInfo(C.Structure):
     _fields_ = [
         ("outer_iterations", C.c_int), ("inner_iterations", C.c_longlong),
         ("initial_residual", C.c_double), ("final_residual", C.c_double),
-        ("relative_residual", C.c_double),
+        ("relative_residual", C.c_double), ("ppcg_inner_steps", C.c_longlong),
     ]
 
 
@@ -98,6 +98,7 @@ def lib():
                                     C.POINTER(OracleResult), C.c_char_p, i]),
             "oracle_num_threads": (i, []),
             "oracle_mixed_solve": (i, [d, d, i, i, C.POINTER(MixedInfo)]),
+            "oracle_mixed_solve_ppcg": (i, [d, d, i, i, i, i, C.POINTER(MixedInfo)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -224,6 +225,14 @@ class Chunk:
         info = MixedInfo()
         if lib().oracle_mixed_solve(tol, inner_tol, max_outer, max_inner, C.byref(info)) != 0:
             raise RuntimeError("oracle mixed solve failed")
+        return info
+
+    def mixed_solve_ppcg(self, tol, inner_tol=1e-4, max_outer=50, max_inner=10000,
+                         presteps=25, inner_steps=10):
+        info = MixedInfo()
+        if lib().oracle_mixed_solve_ppcg(tol, inner_tol, max_outer, max_inner, presteps,
+                                         inner_steps, C.byref(info)) != 0:
+            raise RuntimeError("oracle mixed PPCG solve failed")
         return info
 
     def update_halo(self, fields, depth):

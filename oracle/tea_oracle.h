@@ -125,9 +125,19 @@ typedef struct {
   double initial_residual;
   double final_residual;
   double relative_residual;
+  long long ppcg_inner_steps;
 } oracle_mixed_info;
 int oracle_mixed_solve(double tol, double inner_tol, int max_outer,
                        int max_inner, oracle_mixed_info* info);
+/* restates tea_gb300_mixed_solve_ppcg: FP32 PPCG inner solver */
+int oracle_mixed_solve_ppcg(double tol, double inner_tol, int max_outer, int max_inner,
+                            int presteps, int inner_steps, oracle_mixed_info* info);
+/* eigenvalue range from CG alphas/betas and Chebyshev coefficients
+ * (tea_leaf_cheby.f90:96-172; tea_oracle_driver.c) */
+int oracle_calc_eigenvalues(const double* cg_alphas, const double* cg_betas, int nsteps,
+                            double* eigmin, double* eigmax);
+void oracle_calc_ch_coefs(double* alphas, double* betas, double eigmin, double eigmax,
+                          double* theta, int n);
 
 /* ---- whole runs (restatement of the Fortran driver) ---- */
 typedef struct {

@@ -443,6 +443,16 @@ static void calc_ch_coefs(double* alphas, double* betas, double eigmin,
   *theta_out = theta;
 }
 
+int oracle_calc_eigenvalues(const double* cg_alphas, const double* cg_betas, int nsteps,
+                            double* eigmin, double* eigmax) {
+  return calc_eigenvalues(cg_alphas, cg_betas, nsteps, eigmin, eigmax);
+}
+
+void oracle_calc_ch_coefs(double* alphas, double* betas, double eigmin, double eigmax,
+                          double* theta, int n) {
+  calc_ch_coefs(alphas, betas, eigmin, eigmax, theta, n);
+}
+
 /* ------------------------------------------------------------------------ */
 /* driver                                                                   */
 /* ------------------------------------------------------------------------ */
@@ -573,18 +583,24 @@ static int tea_leaf(Run* R, int step_index) {
 
   if (D->mixed) {
     oracle_mixed_info mi;
-    oracle_mixed_solve(D->eps, D->mixed_inner_eps, D->mixed_max_outer,
-                       D->max_iters, &mi);
-    logf_(R, "Mixed precision: %d FP64 corrections, %lld FP32 CG iterations, "
+    const int ppcg = D->solver == ORC_SOLVER_PPCG;
+    if (ppcg)
+      oracle_mixed_solve_ppcg(D->eps, D->mixed_inner_eps, D->mixed_max_outer,
+                              D->max_iters, D->tl_ch_cg_presteps, D->ppcg_inner_steps, &mi);
+    else
+      oracle_mixed_solve(D->eps, D->mixed_inner_eps, D->mixed_max_outer,
+                         D->max_iters, &mi);
+    logf_(R, "Mixed precision: %d FP64 corrections, %lld FP32 %s iterations, "
              "relative FP64 residual %14.7E\n",
-          mi.outer_iterations, mi.inner_iterations, mi.relative_residual);
+          mi.outer_iterations, mi.inner_iterations, ppcg ? "PPCG" : "CG",
+          mi.relative_residual);
     oracle_finalise_kernel();
     int fe[7] = {0, 0, 1, 0, 0, 0, 0};
     update_halo(R, fe, 1);
     oracle_result* res = R->R;
     if (step_index < 1024) {
       res->iterations[step_index] = (int)mi.inner_iterations;
-      res->inner_iterations[step_index] = 0;
+      res->inner_iterations[step_index] = (int)mi.ppcg_inner_steps;
       res->outer_corrections[step_index] = mi.outer_iterations;
       res->relative_residual[step_index] = mi.relative_residual;
       res->conduction_error[step_index] = mi.final_residual / initial_residual;

@@ -974,14 +974,14 @@ int oracle_num_threads(void) {
  * per lane as an exact float pair (acc_pair), FP64 ones with fma.
  */
 typedef struct {
-  float *Kx, *Ky, *D, *Mi, *d, *r, *p, *w;
+  float *Kx, *Ky, *D, *Mi, *d, *r, *p, *w, *z, *sd;
 } OrcMix;
 static OrcMix M;
 static long M_n = 0;
 
 static void mix_free(void) {
-  float** f[8] = {&M.Kx, &M.Ky, &M.D, &M.Mi, &M.d, &M.r, &M.p, &M.w};
-  for (int i = 0; i < 8; i++) {
+  float** f[10] = {&M.Kx, &M.Ky, &M.D, &M.Mi, &M.d, &M.r, &M.p, &M.w, &M.z, &M.sd};
+  for (int i = 0; i < 10; i++) {
     free(*f[i]);
     *f[i] = NULL;
   }
@@ -991,8 +991,8 @@ static void mix_free(void) {
 static int mix_alloc(void) {
   if (M_n == C.n2 && M.Kx) return 0;
   mix_free();
-  float** f[8] = {&M.Kx, &M.Ky, &M.D, &M.Mi, &M.d, &M.r, &M.p, &M.w};
-  for (int i = 0; i < 8; i++) {
+  float** f[10] = {&M.Kx, &M.Ky, &M.D, &M.Mi, &M.d, &M.r, &M.p, &M.w, &M.z, &M.sd};
+  for (int i = 0; i < 10; i++) {
     *f[i] = (float*)calloc((size_t)C.n2, sizeof(float));
     if (!*f[i]) return -1;
   }
@@ -1040,8 +1040,169 @@ static void mix_residual(double* out) {
                         LANE_FLOAT_PAIR);
 }
 
-int oracle_mixed_solve(double tol, double inner_tol, int max_outer,
-                       int max_inner, oracle_mixed_info* info) {
+/* ---- FP32 inner iterations (the kernels of tea_mixed.cu) ---- */
+
+/* w = A p; returns p.w */
+static double mix_calc_w(void) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      const float wv = smvp32(M.p, c);
+      M.w[c] = wv;
+      DOT(0, col, row, (double)M.p[c], (double)wv);
+    }
+  return reduce_pairs(C.scratch[0], C.scratchb[0], C.x_max, C.y_max, LANE_FLOAT_PAIR);
+}
+
+/* CG: d += a p; r -= a w; returns r.(Mi r) */
+static double mix_cg_ur(float af) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      M.d[c] = fmaf(af, M.p[c], M.d[c]);
+      const float rv = fmaf(-af, M.w[c], M.r[c]);
+      M.r[c] = rv;
+      const float zv = M.Mi[c] * rv;
+      DOT(0, col, row, (double)rv, (double)zv);
+    }
+  return reduce_pairs(C.scratch[0], C.scratchb[0], C.x_max, C.y_max, LANE_FLOAT_PAIR);
+}
+
+/* CG: p = Mi r + b p */
+static void mix_cg_p(float bf) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      M.p[c] = fmaf(bf, M.p[c], M.Mi[c] * M.r[c]);
+    }
+}
+
+/* PPCG: d += a p; r -= a w; z = Mi r */
+static void mix_ppcg_ur(float af) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      const float dv = fmaf(af, M.p[c], M.d[c]);
+      const float rv = fmaf(-af, M.w[c], M.r[c]);
+      M.d[c] = dv;
+      M.r[c] = rv;
+      M.z[c] = M.Mi[c] * rv;
+    }
+}
+
+/* PPCG inner steps: sd = (Mi r)/theta, then per step d += sd, r -= A sd,
+ * sd = a sd + b (Mi r) */
+static void mix_ppcg_inner(float tf, const float* ca, const float* cb, int steps) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      M.sd[c] = (M.Mi[c] * M.r[c]) / tf;
+    }
+  for (int k = 0; k < steps; k++) {
+#pragma omp parallel for schedule(static)
+    for (int row = H; row < H + C.y_max; row++)
+      for (int col = H; col < H + C.x_max; col++) {
+        const long c = IDX(col, row);
+        const float dv = M.d[c] + M.sd[c];
+        const float rv = M.r[c] - smvp32(M.sd, c);
+        M.d[c] = dv;
+        M.r[c] = rv;
+      }
+#pragma omp parallel for schedule(static)
+    for (int row = H; row < H + C.y_max; row++)
+      for (int col = H; col < H + C.x_max; col++) {
+        const long c = IDX(col, row);
+        M.sd[c] = fmaf(ca[k], M.sd[c], cb[k] * (M.Mi[c] * M.r[c]));
+      }
+  }
+}
+
+/* PPCG: r.z with the kept z */
+static double mix_ppcg_rz(void) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      DOT(0, col, row, (double)M.r[c], (double)M.z[c]);
+    }
+  return reduce_pairs(C.scratch[0], C.scratchb[0], C.x_max, C.y_max, LANE_FLOAT_PAIR);
+}
+
+/* PPCG: p = z + b p */
+static void mix_ppcg_p(float bf) {
+  const int H = C.H;
+#pragma omp parallel for schedule(static)
+  for (int row = H; row < H + C.y_max; row++)
+    for (int col = H; col < H + C.x_max; col++) {
+      const long c = IDX(col, row);
+      M.p[c] = fmaf(bf, M.p[c], M.z[c]);
+    }
+}
+
+/* The device loop state of one inner solve (MixState in tea_mixed.cu). */
+typedef struct {
+  double rro, rrn, eps2;
+  int n, max_iters, stop, done;
+  double* alphas; /* CG alpha/beta by iteration number, or NULL */
+  double* betas;
+} MixLoop;
+
+/* CG iterations until the loop stops (k_mix_calc_w/ur/p with the scalar
+ * step of k_mix_calc_ur's last block) */
+static void mix_run_cg(MixLoop* L) {
+  for (;;) {
+    const double pw = mix_calc_w();
+    const double alpha = L->rro / pw;
+    const double rrn = mix_cg_ur((float)alpha);
+    const double beta = rrn / L->rro;
+    if (L->alphas) {
+      L->alphas[L->n] = alpha;
+      L->betas[L->n] = beta;
+    }
+    L->rrn = rrn;
+    L->rro = rrn;
+    L->done = L->n;
+    L->stop = (rrn <= L->eps2 || L->n >= L->max_iters);
+    mix_cg_p((float)beta);
+    if (L->stop) return;
+    L->n++;
+  }
+}
+
+/* PPCG iterations until the loop stops (tea_mixed.cu enqueue_ppcg) */
+static void mix_run_ppcg(MixLoop* L, float tf, const float* ca, const float* cb,
+                         int steps) {
+  for (;;) {
+    const double pw = mix_calc_w();
+    const double alpha = L->rro / pw;
+    mix_ppcg_ur((float)alpha);
+    mix_ppcg_inner(tf, ca, cb, steps);
+    const double rrn = mix_ppcg_rz();
+    const double beta = rrn / L->rro;
+    L->rrn = rrn;
+    L->rro = rrn;
+    L->done = L->n;
+    L->stop = (rrn <= L->eps2 || L->n >= L->max_iters);
+    mix_ppcg_p((float)beta);
+    if (L->stop) return;
+    L->n++;
+  }
+}
+
+static int mixed_solve(double tol, double inner_tol, int max_outer, int max_inner,
+                       int ppcg, int presteps, int inner_steps,
+                       oracle_mixed_info* info) {
   const int H = C.H;
   memset(info, 0, sizeof(*info));
   if (!C_ready || mix_alloc() != 0) return -1;
@@ -1058,59 +1219,77 @@ int oracle_mixed_solve(double tol, double inner_tol, int max_outer,
       M.D[c] = (float)D;
       M.Mi[c] = (float)(1.0 / D);
     }
+  double* ab = NULL;
+  float *ca = NULL, *cb = NULL;
+  float tf = 0.0f;
+  int have_eigs = 0, eig_failed = 0;
+  if (ppcg) {
+    ab = (double*)calloc(2 * (size_t)(presteps + 2), sizeof(double));
+    ca = (float*)calloc((size_t)inner_steps, sizeof(float));
+    cb = (float*)calloc((size_t)inner_steps, sizeof(float));
+  }
   double res[2];
   mix_residual(res);
   const double rr_first = res[0];
   info->initial_residual = sqrt(rr_first);
   int outer = 0;
-  long long inner_total = 0;
+  long long inner_total = 0, cheby_total = 0;
   while (!(sqrt(res[0]) <= tol * sqrt(rr_first)) && outer < max_outer) {
-    double rro = res[1];
+    MixLoop L;
+    memset(&L, 0, sizeof(L));
+    L.rro = res[1];
     const double need = 0.25 * tol * sqrt(rr_first) / sqrt(res[0]);
     const double itol = need > inner_tol ? (need < 0.5 ? need : 0.5) : inner_tol;
-    const double eps2 = itol * itol * res[1];
-    int n = 1, done = 0;
-    for (;;) {
-      /* w = A p, p.w */
-#pragma omp parallel for schedule(static)
-      for (int row = H; row < H + C.y_max; row++)
-        for (int col = H; col < H + C.x_max; col++) {
-          const long c = IDX(col, row);
-          const float wv = smvp32(M.p, c);
-          M.w[c] = wv;
-          DOT(0, col, row, (double)M.p[c], (double)wv);
+    L.eps2 = itol * itol * res[1];
+    L.n = 1;
+    L.max_iters = max_inner;
+    int use_ppcg = ppcg && have_eigs;
+    if (ppcg && !have_eigs && !eig_failed) {
+      /* CG presteps, then the eigenvalue range (tea_solve.f90:175-210) */
+      L.max_iters = presteps < max_inner ? presteps : max_inner;
+      L.alphas = ab;
+      L.betas = ab + presteps + 2;
+      mix_run_cg(&L);
+      const int converged = L.rrn <= L.eps2;
+      L.alphas = L.betas = NULL;
+      if (!converged && L.done < max_inner) {
+        const int n = L.done;
+        double eigmin = 0.0, eigmax = 0.0;
+        if (oracle_calc_eigenvalues(ab + 1, ab + presteps + 3, n, &eigmin, &eigmax) != 0) {
+          eig_failed = 1;
+        } else {
+          double* cha = (double*)calloc((size_t)inner_steps, sizeof(double));
+          double* chb = (double*)calloc((size_t)inner_steps, sizeof(double));
+          double theta = 0.0;
+          oracle_calc_ch_coefs(cha, chb, eigmin * 0.95, eigmax * 1.05, &theta, inner_steps);
+          for (int k = 0; k < inner_steps; k++) {
+            ca[k] = (float)cha[k];
+            cb[k] = (float)chb[k];
+          }
+          tf = (float)theta;
+          free(cha);
+          free(chb);
+          have_eigs = 1;
+          use_ppcg = 1;
         }
-      const double pw = reduce_pairs(C.scratch[0], C.scratchb[0], C.x_max, C.y_max,
-                                     LANE_FLOAT_PAIR);
-      const double alpha = rro / pw;
-      const float af = (float)alpha;
-#pragma omp parallel for schedule(static)
-      for (int row = H; row < H + C.y_max; row++)
-        for (int col = H; col < H + C.x_max; col++) {
-          const long c = IDX(col, row);
-          M.d[c] = fmaf(af, M.p[c], M.d[c]);
-          const float rv = fmaf(-af, M.w[c], M.r[c]);
-          M.r[c] = rv;
-          const float zv = M.Mi[c] * rv;
-          DOT(0, col, row, (double)rv, (double)zv);
+        L.stop = 0;
+        L.n = n + 1;
+        L.max_iters = max_inner;
+        const int pre = L.done;
+        if (use_ppcg) {
+          mix_run_ppcg(&L, tf, ca, cb, inner_steps);
+          cheby_total += (long long)(L.done - pre) * inner_steps;
+        } else {
+          mix_run_cg(&L);
         }
-      const double rrn = reduce_pairs(C.scratch[0], C.scratchb[0], C.x_max, C.y_max,
-                                      LANE_FLOAT_PAIR);
-      const double beta = rrn / rro;
-      rro = rrn;
-      done = n;
-      const int stop = (rrn <= eps2 || n >= max_inner);
-      const float bf = (float)beta;
-#pragma omp parallel for schedule(static)
-      for (int row = H; row < H + C.y_max; row++)
-        for (int col = H; col < H + C.x_max; col++) {
-          const long c = IDX(col, row);
-          M.p[c] = fmaf(bf, M.p[c], M.Mi[c] * M.r[c]);
-        }
-      if (stop) break;
-      n++;
+      }
+    } else if (use_ppcg) {
+      mix_run_ppcg(&L, tf, ca, cb, inner_steps);
+      cheby_total += (long long)L.done * inner_steps;
+    } else {
+      mix_run_cg(&L);
     }
-    inner_total += done;
+    inner_total += L.done;
 #pragma omp parallel for schedule(static)
     for (int row = H; row < H + C.y_max; row++)
       for (int col = H; col < H + C.x_max; col++) {
@@ -1120,9 +1299,24 @@ int oracle_mixed_solve(double tol, double inner_tol, int max_outer,
     outer++;
     mix_residual(res);
   }
+  free(ab);
+  free(ca);
+  free(cb);
   info->outer_iterations = outer;
   info->inner_iterations = inner_total;
+  info->ppcg_inner_steps = cheby_total;
   info->final_residual = sqrt(res[0]);
   info->relative_residual = sqrt(res[0]) / sqrt(rr_first);
   return 0;
+}
+
+int oracle_mixed_solve(double tol, double inner_tol, int max_outer,
+                       int max_inner, oracle_mixed_info* info) {
+  return mixed_solve(tol, inner_tol, max_outer, max_inner, 0, 0, 0, info);
+}
+
+int oracle_mixed_solve_ppcg(double tol, double inner_tol, int max_outer, int max_inner,
+                            int presteps, int inner_steps, oracle_mixed_info* info) {
+  if (presteps < 1 || inner_steps < 1) return -1;
+  return mixed_solve(tol, inner_tol, max_outer, max_inner, 1, presteps, inner_steps, info);
 }

@@ -681,18 +681,23 @@ class Driver {
     (void)rx;
     (void)ry;
     tea_gb300_mixed_info mi;
-    if (tea_gb300_mixed_solve(D.eps, D.mixed_inner_eps, D.mixed_max_outer,
-                              D.max_iters, &mi) != 0)
-      return -1;
-    say("Mixed precision: %d FP64 corrections, %lld FP32 CG iterations, "
+    const bool ppcg = D.solver == TEA_SOLVER_PPCG;
+    const int rc = ppcg ? tea_gb300_mixed_solve_ppcg(D.eps, D.mixed_inner_eps,
+                                                     D.mixed_max_outer, D.max_iters,
+                                                     D.presteps, D.inner_steps, &mi)
+                        : tea_gb300_mixed_solve(D.eps, D.mixed_inner_eps,
+                                                D.mixed_max_outer, D.max_iters, &mi);
+    if (rc != 0) return -1;
+    say("Mixed precision: %d FP64 corrections, %lld FP32 %s iterations, "
         "relative FP64 residual %14.7E\n",
-        mi.outer_iterations, mi.inner_iterations, mi.relative_residual);
+        mi.outer_iterations, mi.inner_iterations, ppcg ? "PPCG" : "CG",
+        mi.relative_residual);
     tea_leaf_common_finalise_kernel_ocl_();
     const int fe[7] = {0, 0, 1, 0, 0, 0, 0};
     update_halo(fe, 1);
     if (info) {
       info->iterations = (int)mi.inner_iterations;
-      info->inner_iterations = 0;
+      info->inner_iterations = (int)mi.ppcg_inner_steps;
       info->outer_corrections = mi.outer_iterations;
       info->relative_residual = mi.relative_residual;
       info->conduction_error = mi.final_residual / initial_residual;
@@ -738,6 +743,18 @@ class Driver {
 Driver* g_driver = nullptr;
 
 }  // namespace
+
+namespace tea {
+int eigenvalues_from_cg(const std::vector<double>& alphas,
+                        const std::vector<double>& betas, int nsteps,
+                        double* eigmin, double* eigmax) {
+  return calc_eigenvalues(alphas, betas, nsteps, eigmin, eigmax);
+}
+void chebyshev_coefficients(std::vector<double>& a, std::vector<double>& b,
+                            double eigmin, double eigmax, double* theta, int n) {
+  calc_ch_coefs(a, b, eigmin, eigmax, theta, n);
+}
+}  // namespace tea
 
 extern "C" int tea_gb300_driver_open(const char* deck_text,
                                      const char* log_path, int mode,

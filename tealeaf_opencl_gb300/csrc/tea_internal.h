@@ -16,6 +16,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 namespace tea {
 
@@ -205,6 +206,13 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
 void resident_release();
 // mixed-precision solve (tea_mixed.cu)
 void mixed_release();
+// eigenvalue range from CG alphas/betas (nsteps of each, iteration 1
+// first) and Chebyshev coefficients (tea_driver.cpp; tea_leaf_cheby.f90)
+int eigenvalues_from_cg(const std::vector<double>& alphas,
+                        const std::vector<double>& betas, int nsteps,
+                        double* eigmin, double* eigmax);
+void chebyshev_coefficients(std::vector<double>& a, std::vector<double>& b,
+                            double eigmin, double eigmax, double* theta, int n);
 // FP64 fused-multiply-add instructions per second of this GPU
 double measure_fp64_rate();
 

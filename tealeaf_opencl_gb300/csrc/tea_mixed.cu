@@ -27,6 +27,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "../../include/tealeaf_gb300.h"
 #include "tea_device.cuh"
@@ -38,6 +39,7 @@ namespace tea {
 struct MixDev {
   long long S;  // row stride in floats
   float *Kx, *Ky, *D, *Mi, *d, *r, *p, *w;
+  float *z, *sd;  // PPCG: the kept M^-1 r and the inner direction
 };
 
 struct MixState {
@@ -45,13 +47,15 @@ struct MixState {
   double eps2;  // (inner relative tolerance)^2 * rz0
   int n, max_iters, stop, p_pending;
   int done_iters, pad;
+  double* alphas;  // CG alpha and beta by iteration number (PPCG presteps)
+  double* betas;
 };
 
 struct MixChunk {
   bool ready = false;
   int x_max = 0, y_max = 0, H = 0;
   long long S = 0;
-  float* base[8] = {nullptr};
+  float* base[10] = {nullptr};
   MixDev dev{};
   MixState* st = nullptr;    // device
   MixState* st_h = nullptr;  // pinned
@@ -232,6 +236,10 @@ __global__ void __launch_bounds__(kBlock, kMixMinBlocks)
     const double rrn = red.result[0];
     st->alpha = alpha;
     st->beta = rrn / st->rro;
+    if (st->alphas) {
+      st->alphas[st->n] = alpha;
+      st->betas[st->n] = st->beta;
+    }
     st->rrn = rrn;
     st->rro = rrn;
     st->p_pending = 1;
@@ -263,6 +271,138 @@ __global__ void __launch_bounds__(kBlock, kMixMinBlocks)
 #pragma unroll
     for (int j = 0; j < TH; j++)
       if (y0 + j < d.y_max) m.p[cidx32(d, m, x, y0 + j)] = pv[j];
+  });
+  if (last_block(counter) && threadIdx.x == 0) {
+    st->p_pending = 0;
+    __threadfence();
+  }
+}
+
+// ---- FP32 PPCG inner solve (the FP64 driver's tea_leaf PPCG branch,
+// tea_solve.f90:240-268 and :422-475, restated in FP32 with diagonal
+// Jacobi): after the CG presteps, one iteration is calc_w, the u/r update
+// keeping z = M^-1 r, inner_steps Chebyshev steps on d and r, r.z with the
+// kept z, and p = z + beta p.
+
+// d += alpha p; r -= alpha w; z = Mi r (no sum: PPCG takes r.z after its
+// inner steps)
+template <int TH>
+__global__ void __launch_bounds__(kBlock, kMixMinBlocks)
+    k_mix_ppcg_ur(Dev d, MixDev m, Red red, MixState* st) {
+  if (*(volatile int*)&st->stop) return;
+  const double alpha = st->rro / st->pw;
+  const float af = (float)alpha;
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 1
+    for (int y = y0; y < y0 + TH && y < d.y_max; y++) {
+      const long long c3 = cidx32(d, m, x, y);
+      const float dv = __fmaf_rn(af, m.p[c3], m.d[c3]);
+      const float rv = __fmaf_rn(-af, m.w[c3], m.r[c3]);
+      m.d[c3] = dv;
+      m.r[c3] = rv;
+      m.z[c3] = m.Mi[c3] * rv;
+    }
+  });
+}
+
+// sd = (Mi r) / theta (tea_leaf_ppcg_solve_init_sd)
+template <int TH>
+__global__ void __launch_bounds__(kBlock, kMixMinBlocks)
+    k_mix_ppcg_init_sd(Dev d, MixDev m, Red red, MixState* st, float theta) {
+  if (*(volatile int*)&st->stop) return;
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 1
+    for (int y = y0; y < y0 + TH && y < d.y_max; y++) {
+      const long long c3 = cidx32(d, m, x, y);
+      m.sd[c3] = (m.Mi[c3] * m.r[c3]) / theta;
+    }
+  });
+}
+
+// d += sd; r -= A sd (tea_leaf_ppcg_solve_update_r)
+template <int TH>
+__global__ void __launch_bounds__(kBlock, kMixMinBlocks)
+    k_mix_ppcg_update_r(Dev d, MixDev m, Red red, MixState* st) {
+  if (*(volatile int*)&st->stop) return;
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 1
+    for (int y = y0; y < y0 + TH && y < d.y_max; y++) {
+      const long long c3 = cidx32(d, m, x, y);
+      const float dv = m.d[c3] + m.sd[c3];
+      const float rv = m.r[c3] - smvp32(m, m.sd, c3);
+      m.d[c3] = dv;
+      m.r[c3] = rv;
+    }
+  });
+}
+
+// sd = a sd + b (Mi r) (tea_leaf_ppcg_solve_calc_sd)
+template <int TH>
+__global__ void __launch_bounds__(kBlock, kMixMinBlocks)
+    k_mix_ppcg_calc_sd(Dev d, MixDev m, Red red, MixState* st, float a, float b) {
+  if (*(volatile int*)&st->stop) return;
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 1
+    for (int y = y0; y < y0 + TH && y < d.y_max; y++) {
+      const long long c3 = cidx32(d, m, x, y);
+      m.sd[c3] = __fmaf_rn(a, m.sd[c3], b * (m.Mi[c3] * m.r[c3]));
+    }
+  });
+}
+
+// r.z with the z kept by k_mix_ppcg_ur; the last block takes the scalar
+// step and the exit test of the iteration
+template <int TH>
+__global__ void __launch_bounds__(kBlock, kMixMinBlocks)
+    k_mix_ppcg_rz(Dev d, MixDev m, Red red, MixState* st) {
+  if (*(volatile int*)&st->stop) return;
+  const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    float hi = 0.0f, lo = 0.0f;
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      float rv = 0.0f, zv = 0.0f;
+      if (xin && y < d.y_max) {
+        const long long c3 = cidx32(d, m, x, y);
+        rv = m.r[c3];
+        zv = m.z[c3];
+      }
+      acc_pair(hi, lo, rv, zv);
+    }
+    acc[0] = pair_value(hi, lo);
+  });
+  if (last && threadIdx.x == 0) {
+    const double rrn = red.result[0];
+    st->beta = rrn / st->rro;
+    st->rrn = rrn;
+    st->rro = rrn;
+    st->p_pending = 1;
+    st->done_iters = st->n;
+    if (rrn <= st->eps2 || st->n >= st->max_iters)
+      st->stop = 1;
+    else
+      st->n = st->n + 1;
+    __threadfence();
+  }
+}
+
+// p = z + beta p with the kept z
+template <int TH>
+__global__ void __launch_bounds__(kBlock, kMixMinBlocks)
+    k_mix_ppcg_calc_p(Dev d, MixDev m, Red red, MixState* st, unsigned int* counter) {
+  if (!*(volatile int*)&st->p_pending) return;
+  const float bf = (float)st->beta;
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 1
+    for (int y = y0; y < y0 + TH && y < d.y_max; y++) {
+      const long long c3 = cidx32(d, m, x, y);
+      m.p[c3] = __fmaf_rn(bf, m.p[c3], m.z[c3]);
+    }
   });
   if (last_block(counter) && threadIdx.x == 0) {
     st->p_pending = 0;
@@ -338,9 +478,9 @@ static bool mixed_alloc(Chunk& c) {
   g.S = ((long long)(c.x_max + 2 * c.H + 1 + 63) / 64) * 64;
   const long long off = (64 - (c.H % 64)) % 64;
   const size_t n = (size_t)(off + (c.y_max + 2 * c.H + 1) * g.S + 64);
-  float** f[8] = {&g.dev.Kx, &g.dev.Ky, &g.dev.D, &g.dev.Mi,
-                  &g.dev.d,  &g.dev.r,  &g.dev.p, &g.dev.w};
-  for (int i = 0; i < 8; i++) {
+  float** f[10] = {&g.dev.Kx, &g.dev.Ky, &g.dev.D, &g.dev.Mi, &g.dev.d,
+                   &g.dev.r,  &g.dev.p,  &g.dev.w, &g.dev.z,  &g.dev.sd};
+  for (int i = 0; i < 10; i++) {
     if (!check_cuda(cudaMalloc(&g.base[i], n * sizeof(float)), "cudaMalloc mixed field"))
       return false;
     cudaMemsetAsync(g.base[i], 0, n * sizeof(float), c.stream);
@@ -357,27 +497,90 @@ static bool mixed_alloc(Chunk& c) {
 }
 
 template <int TH>
+static void enqueue_ppcg(Chunk& c, int iters, float theta, const std::vector<float>& ca,
+                         const std::vector<float>& cb) {
+  const Dev d = c.dev();
+  const Red red = c.red();
+  const MixDev m = g_mix.dev;
+  MixState* st = g_mix.st;
+  const int gw = mix_grid(c, k_mix_calc_w<TH>);
+  const int gu = mix_grid(c, k_mix_ppcg_ur<TH>);
+  const int gs = mix_grid(c, k_mix_ppcg_init_sd<TH>);
+  const int gr = mix_grid(c, k_mix_ppcg_update_r<TH>);
+  const int gd = mix_grid(c, k_mix_ppcg_calc_sd<TH>);
+  const int gz = mix_grid(c, k_mix_ppcg_rz<TH>);
+  const int gp = mix_grid(c, k_mix_ppcg_calc_p<TH>);
+  for (int i = 0; i < iters; i++) {
+    k_mix_calc_w<TH><<<gw, kBlock, 0, c.stream>>>(d, m, red, st);
+    k_mix_ppcg_ur<TH><<<gu, kBlock, 0, c.stream>>>(d, m, red, st);
+    k_mix_ppcg_init_sd<TH><<<gs, kBlock, 0, c.stream>>>(d, m, red, st, theta);
+    for (size_t k = 0; k < ca.size(); k++) {
+      k_mix_ppcg_update_r<TH><<<gr, kBlock, 0, c.stream>>>(d, m, red, st);
+      k_mix_ppcg_calc_sd<TH><<<gd, kBlock, 0, c.stream>>>(d, m, red, st, ca[k], cb[k]);
+    }
+    k_mix_ppcg_rz<TH><<<gz, kBlock, 0, c.stream>>>(d, m, red, st);
+    k_mix_ppcg_calc_p<TH><<<gp, kBlock, 0, c.stream>>>(d, m, red, st, g_mix.counter);
+  }
+}
+
+// Captures `enqueue` on the chunk's stream into an executable graph.
+template <class F>
+static cudaGraphExec_t mix_capture(Chunk& c, F enqueue) {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  if (!check_cuda(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal),
+                  "mixed graph capture"))
+    return nullptr;
+  enqueue();
+  if (!check_cuda(cudaStreamEndCapture(c.stream, &graph), "mixed graph capture end"))
+    return nullptr;
+  const bool ok = check_cuda(cudaGraphInstantiate(&exec, graph, 0), "mixed graph instantiate");
+  cudaGraphDestroy(graph);
+  return ok ? exec : nullptr;
+}
+
+// Uploads h, replays `graph` (iters_per_replay iterations, `kernels`
+// kernels each) until the inner loop has stopped, and reads h back.
+static bool run_inner(Chunk& c, cudaGraphExec_t graph, int iters_per_replay, int kernels,
+                      MixState& h) {
+  MixChunk& g = g_mix;
+  if (!check_cuda(cudaMemcpyAsync(g.st, &h, sizeof(MixState), cudaMemcpyHostToDevice,
+                                  c.stream),
+                  "mixed state upload"))
+    return false;
+  const long long max_batches = (long long)(h.max_iters - h.n) / iters_per_replay + 3;
+  for (long long nb = 0;; nb++) {
+    if (nb >= max_batches) {
+      fail(40, "mixed inner loop did not stop after %lld batches", nb);
+      return false;
+    }
+    if (!check_cuda(cudaGraphLaunch(graph, c.stream), "mixed graph launch")) return false;
+    count_launches(kernels);
+    if (!check_cuda(cudaMemcpyAsync(&h, g.st, sizeof(MixState), cudaMemcpyDeviceToHost,
+                                    c.stream),
+                    "mixed state read") ||
+        !check_cuda(cudaStreamSynchronize(c.stream), "mixed sync"))
+      return false;
+    if (h.stop && !h.p_pending) return true;
+  }
+}
+
+template <int TH>
 static bool mixed_solve_t(Chunk& c, double tol, double inner_tol, int max_outer,
-                          int max_inner, tea_gb300_mixed_info* info) {
+                          int max_inner, int solver, int presteps, int inner_steps,
+                          tea_gb300_mixed_info* info) {
   MixChunk& g = g_mix;
   const Dev d = c.dev();
   const Red red = c.red();
-  const int batch = 16;
+  const int batch = 16, ppcg_batch = 4;
   {
     const dim3 block(32, 8), grid((d.xs + 1 + 31) / 32, (d.ys + 1 + 7) / 8);
     k_mix_convert<<<grid, block, 0, c.stream>>>(d, g.dev);
     count_launch("mixed_convert");
   }
   if (!g.graph) {
-    cudaGraph_t graph = nullptr;
-    if (!check_cuda(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal),
-                    "mixed graph capture"))
-      return false;
-    enqueue_inner<TH>(c, batch);
-    if (!check_cuda(cudaStreamEndCapture(c.stream, &graph), "mixed graph capture end") ||
-        !check_cuda(cudaGraphInstantiate(&g.graph, graph, 0), "mixed graph instantiate"))
-      return false;
-    cudaGraphDestroy(graph);
+    g.graph = mix_capture(c, [&]() { enqueue_inner<TH>(c, batch); });
+    if (!g.graph) return false;
     g.graph_batch = batch;
   }
   double res[2];
@@ -393,13 +596,27 @@ static bool mixed_solve_t(Chunk& c, double tol, double inner_tol, int max_outer,
     out[1] = c.host_result[1];
     return true;
   };
-  if (!outer_residual(res)) return false;
+  // PPCG: the first correction's CG presteps give the eigenvalue range
+  // (tea_solve.f90:175-210), kept for the later corrections of this call
+  const bool ppcg = solver == SOLVER_PPCG;
+  bool have_eigs = false, eig_failed = false;
+  double* coef_d = nullptr;
+  cudaGraphExec_t ppcg_graph = nullptr;
+  auto cleanup = [&](bool ok) {
+    if (ppcg_graph) cudaGraphExecDestroy(ppcg_graph);
+    cudaFree(coef_d);
+    return ok;
+  };
+  if (ppcg && !check_cuda(cudaMalloc(&coef_d, 2 * sizeof(double) * (presteps + 2)),
+                          "cudaMalloc mixed coefficients"))
+    return false;
+  if (!outer_residual(res)) return cleanup(false);
   const double rr_first = res[0];
   info->initial_residual = sqrt(rr_first);
   int outer = 0;
-  long long inner_total = 0;
+  long long inner_total = 0, cheby_total = 0;
   while (!(sqrt(res[0]) <= tol * sqrt(rr_first)) && outer < max_outer) {
-    MixState& h = *g.st_h;
+    MixState h;
     memset(&h, 0, sizeof(h));
     h.rro = res[1];
     h.rz0 = res[1];
@@ -410,57 +627,121 @@ static bool mixed_solve_t(Chunk& c, double tol, double inner_tol, int max_outer,
     h.eps2 = itol * itol * res[1];
     h.n = 1;
     h.max_iters = max_inner;
-    if (!check_cuda(cudaMemcpyAsync(g.st, &h, sizeof(MixState), cudaMemcpyHostToDevice,
-                                    c.stream),
-                    "mixed state upload"))
-      return false;
-    const long long max_batches = max_inner / batch + 3;
-    for (long long nb = 0;; nb++) {
-      if (nb >= max_batches) {
-        fail(40, "mixed inner loop did not stop after %lld batches", nb);
-        return false;
+    bool use_ppcg = ppcg && have_eigs;
+    if (ppcg && !have_eigs && !eig_failed) {
+      h.max_iters = std::min(presteps, max_inner);
+      h.alphas = coef_d;
+      h.betas = coef_d + presteps + 2;
+      if (!run_inner(c, g.graph, batch, 3 * batch, h)) return cleanup(false);
+      const bool converged = h.rrn <= h.eps2;
+      if (!converged && h.done_iters < max_inner) {
+        const int n = h.done_iters;
+        std::vector<double> ab(2 * (presteps + 2));
+        if (!check_cuda(cudaMemcpy(ab.data(), coef_d, ab.size() * sizeof(double),
+                                   cudaMemcpyDeviceToHost),
+                        "mixed coefficients read"))
+          return cleanup(false);
+        const std::vector<double> a(ab.begin() + 1, ab.begin() + 1 + n);
+        const std::vector<double> b(ab.begin() + presteps + 3,
+                                    ab.begin() + presteps + 3 + n);
+        double eigmin = 0.0, eigmax = 0.0;
+        if (eigenvalues_from_cg(a, b, n, &eigmin, &eigmax) != 0) {
+          eig_failed = true;  // the rest of the solve stays CG
+        } else {
+          std::vector<double> cha, chb;
+          double theta = 0.0;
+          chebyshev_coefficients(cha, chb, eigmin * 0.95, eigmax * 1.05, &theta,
+                                 inner_steps);
+          std::vector<float> ca(inner_steps), cb(inner_steps);
+          for (int k = 0; k < inner_steps; k++) {
+            ca[k] = (float)cha[k];
+            cb[k] = (float)chb[k];
+          }
+          const float tf = (float)theta;
+          ppcg_graph = mix_capture(c, [&]() { enqueue_ppcg<TH>(c, ppcg_batch, tf, ca, cb); });
+          if (!ppcg_graph) return cleanup(false);
+          have_eigs = true;
+          use_ppcg = true;
+        }
+        // continue this inner solve from where the presteps stopped
+        h.stop = 0;
+        h.n = n + 1;
+        h.max_iters = max_inner;
       }
-      if (!check_cuda(cudaGraphLaunch(g.graph, c.stream), "mixed graph launch")) return false;
-      for (int i = 0; i < 3 * batch; i++) count_launch("mixed_inner");
-      if (!check_cuda(cudaMemcpyAsync(&h, g.st, sizeof(MixState), cudaMemcpyDeviceToHost,
-                                      c.stream),
-                      "mixed state read") ||
-          !check_cuda(cudaStreamSynchronize(c.stream), "mixed sync"))
-        return false;
-      if (h.stop && !h.p_pending) break;
+      h.alphas = h.betas = nullptr;
+      if (h.stop) {
+        inner_total += h.done_iters;
+      } else {
+        const int pre = h.done_iters;
+        if (use_ppcg) {
+          if (!run_inner(c, ppcg_graph, ppcg_batch, ppcg_batch * (5 + 2 * inner_steps), h))
+            return cleanup(false);
+          cheby_total += (long long)(h.done_iters - pre) * inner_steps;
+        } else if (!run_inner(c, g.graph, batch, 3 * batch, h)) {
+          return cleanup(false);
+        }
+        inner_total += h.done_iters;
+      }
+    } else {
+      if (use_ppcg) {
+        if (!run_inner(c, ppcg_graph, ppcg_batch, ppcg_batch * (5 + 2 * inner_steps), h))
+          return cleanup(false);
+        cheby_total += (long long)h.done_iters * inner_steps;
+      } else if (!run_inner(c, g.graph, batch, 3 * batch, h)) {
+        return cleanup(false);
+      }
+      inner_total += h.done_iters;
     }
-    inner_total += h.done_iters;
     k_mix_update_u<TH><<<mix_grid(c, k_mix_update_u<TH>), kBlock, 0, c.stream>>>(d, g.dev, red);
     count_launch("mixed_update_u");
     outer++;
-    if (!outer_residual(res)) return false;
+    if (!outer_residual(res)) return cleanup(false);
   }
   info->outer_iterations = outer;
   info->inner_iterations = inner_total;
+  info->ppcg_inner_steps = cheby_total;
   info->final_residual = sqrt(res[0]);
   info->relative_residual = sqrt(res[0]) / sqrt(rr_first);
-  return true;
+  return cleanup(true);
 }
 
 }  // namespace tea
 
 using namespace tea;
 
-extern "C" int tea_gb300_mixed_solve(double tol, double inner_tol, int max_outer,
-                                     int max_inner, tea_gb300_mixed_info* info) {
+static int mixed_entry(double tol, double inner_tol, int max_outer, int max_inner,
+                       int solver, int presteps, int inner_steps,
+                       tea_gb300_mixed_info* info, const char* who) {
   Chunk& c = chunk();
   if (!c.ready) {
-    fail(5, "tea_gb300_mixed_solve called before initialise_ocl_");
+    fail(5, "%s called before initialise_ocl_", who);
     return -1;
   }
   if (!(tol > 0.0) || !(inner_tol > 0.0) || inner_tol >= 1.0 || max_outer < 1 ||
-      max_inner < 1 || !info) {
-    fail(41, "tea_gb300_mixed_solve: invalid arguments");
+      max_inner < 1 || !info ||
+      (solver == SOLVER_PPCG && (presteps < 1 || inner_steps < 1 || inner_steps > 1000))) {
+    fail(41, "%s: invalid arguments", who);
     return -1;
   }
   memset(info, 0, sizeof(*info));
   if (!mixed_alloc(c)) return -1;
-  const bool ok = c.TH == 16 ? mixed_solve_t<16>(c, tol, inner_tol, max_outer, max_inner, info)
-                             : mixed_solve_t<4>(c, tol, inner_tol, max_outer, max_inner, info);
+  const bool ok =
+      c.TH == 16 ? mixed_solve_t<16>(c, tol, inner_tol, max_outer, max_inner, solver,
+                                     presteps, inner_steps, info)
+                 : mixed_solve_t<4>(c, tol, inner_tol, max_outer, max_inner, solver,
+                                    presteps, inner_steps, info);
   return ok ? 0 : -1;
+}
+
+extern "C" int tea_gb300_mixed_solve(double tol, double inner_tol, int max_outer,
+                                     int max_inner, tea_gb300_mixed_info* info) {
+  return mixed_entry(tol, inner_tol, max_outer, max_inner, SOLVER_CG, 0, 0, info,
+                     "tea_gb300_mixed_solve");
+}
+
+extern "C" int tea_gb300_mixed_solve_ppcg(double tol, double inner_tol, int max_outer,
+                                          int max_inner, int presteps, int inner_steps,
+                                          tea_gb300_mixed_info* info) {
+  return mixed_entry(tol, inner_tol, max_outer, max_inner, SOLVER_PPCG, presteps,
+                     inner_steps, info, "tea_gb300_mixed_solve_ppcg");
 }

@@ -42,7 +42,7 @@ EXTRA_SYMBOLS = [
     "tea_gb300_synchronize", "tea_gb300_host_alloc", "tea_gb300_host_free",
     "tea_gb300_kernel_timer_select", "tea_gb300_kernel_timer_read",
     "tea_gb300_kernel_timer_read_name", "tea_gb300_fp64_rate",
-    "tea_gb300_dot_noalloc", "tea_gb300_mixed_solve",
+    "tea_gb300_dot_noalloc", "tea_gb300_mixed_solve", "tea_gb300_mixed_solve_ppcg",
     "tea_gb300_driver_open", "tea_gb300_driver_step", "tea_gb300_driver_close",
     "tea_gb300_batch_create", "tea_gb300_batch_set_fields", "tea_gb300_batch_run",
     "tea_gb300_batch_summary", "tea_gb300_batch_iterations",
@@ -72,7 +72,7 @@ class MixedInfo(C.Structure):
     _fields_ = [
         ("outer_iterations", C.c_int), ("inner_iterations", C.c_longlong),
         ("initial_residual", C.c_double), ("final_residual", C.c_double),
-        ("relative_residual", C.c_double),
+        ("relative_residual", C.c_double), ("ppcg_inner_steps", C.c_longlong),
     ]
 
 
@@ -185,6 +185,7 @@ def load(build=True):
         "tea_gb300_dot_noalloc": (i, [C.c_void_p, C.c_void_p, i, i, i, C.c_longlong,
                                       C.c_void_p, C.c_void_p]),
         "tea_gb300_mixed_solve": (i, [d, d, i, i, C.POINTER(MixedInfo)]),
+        "tea_gb300_mixed_solve_ppcg": (i, [d, d, i, i, i, i, C.POINTER(MixedInfo)]),
         "tea_gb300_driver_open": (i, [C.c_char_p, C.c_char_p, i, i]),
         "tea_gb300_driver_step": (i, [C.POINTER(StepInfo)]),
         "tea_gb300_driver_close": (v, []),
@@ -352,6 +353,15 @@ class Chunk:
                                         C.byref(info)) != 0:
             check()
             raise TeaError("mixed solve failed")
+        return info
+
+    def mixed_solve_ppcg(self, tol, inner_tol=1e-4, max_outer=50, max_inner=10000,
+                         presteps=25, inner_steps=10):
+        info = MixedInfo()
+        if load().tea_gb300_mixed_solve_ppcg(tol, inner_tol, max_outer, max_inner, presteps,
+                                             inner_steps, C.byref(info)) != 0:
+            check()
+            raise TeaError("mixed PPCG solve failed")
         return info
 
     def update_halo(self, fields, depth):

@@ -15,9 +15,11 @@ from tealeaf_opencl_gb300 import decks, lib
 pytestmark = pytest.mark.gpu
 
 
-def mixed_deck(cells, steps=3, eps=1e-10, inner=1e-5, y_cells=None, extra=""):
-    return decks.five_state_deck(cells, solver="cg", prec="jac_diag", steps=steps, eps=eps,
-                                 max_iters=20000, y_cells=y_cells,
+def mixed_deck(cells, steps=3, eps=1e-10, inner=1e-5, y_cells=None, extra="",
+               solver="cg", inner_steps=None, presteps=None):
+    return decks.five_state_deck(cells, solver=solver, prec="jac_diag", steps=steps, eps=eps,
+                                 max_iters=20000, y_cells=y_cells, inner_steps=inner_steps,
+                                 presteps=presteps,
                                  extra="tl_mixed_precision\ntl_mixed_inner_eps %g\n%s"
                                  % (inner, extra))
 
@@ -62,3 +64,24 @@ def test_true_residual_exit_reaches_target():
     for s, p in zip(steps, plain):
         assert s.exact_error < 1.1e-10          # recurrence vs recomputed residual
         assert s.iterations >= p.iterations     # a stricter test on this problem
+
+
+@pytest.mark.parametrize("cells,y_cells,inner,inner_steps,presteps",
+                         [(130, 129, 1e-5, 10, 25), (200, 97, 1e-4, 6, 12)])
+def test_mixed_ppcg_matches_oracle(cells, y_cells, inner, inner_steps, presteps):
+    """FP32 PPCG inner solver: CG presteps, eigenvalue range, Chebyshev
+    inner steps; bit for bit against the oracle's restatement."""
+    deck = mixed_deck(cells, y_cells=y_cells, inner=inner, solver="ppcg",
+                      inner_steps=inner_steps, presteps=presteps)
+    steps = lib.run_deck(deck)
+    res = oracle.run_deck(deck)
+    n = res.n_steps
+    assert [s.iterations for s in steps] == list(res.iterations[:n])
+    assert [s.inner_iterations for s in steps] == list(res.inner_iterations[:n])
+    assert all(s.inner_iterations > 0 for s in steps)  # the PPCG phase ran
+    assert [s.outer_corrections for s in steps] == list(res.outer_corrections[:n])
+    assert [s.relative_residual for s in steps] == list(res.relative_residual[:n])
+    final = res.summaries()[-1]
+    last = steps[-1]
+    assert (last.vol, last.mass, last.ie, last.temp) == tuple(final[[1, 2, 4, 5]])
+    assert all(s.relative_residual <= 1e-10 for s in steps)

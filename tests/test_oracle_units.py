@@ -155,3 +155,28 @@ def test_reduction_rows_rule():
     assert oracle.lib().oracle_reduction_rows(4096, 4096) == 16
     assert oracle.lib().oracle_reduction_rows(512, 512) == 4
     assert oracle.lib().oracle_reduction_rows(3840, 3840) == 16
+
+
+@pytest.mark.parametrize("solver", ["cg", "ppcg"])
+def test_mixed_solve_reaches_fp64_tolerance(solver):
+    """The oracle's mixed-precision solve (FP32 CG or PPCG inner, FP64
+    defect correction) reaches the FP64 relative residual it is asked for,
+    and its answer agrees with the FP64 CG solve to the accuracy that
+    residual implies."""
+    from tealeaf_opencl_gb300 import decks
+    extra = "tl_mixed_precision\ntl_mixed_inner_eps 1e-5"
+    kw = dict(solver=solver, prec="jac_diag", steps=2, eps=1e-10, max_iters=20000,
+              summary_frequency=0, y_cells=61)
+    if solver == "ppcg":
+        kw.update(inner_steps=8, presteps=15)
+    mixed = oracle.run_deck(decks.five_state_deck(72, extra=extra, **kw))
+    kw["solver"] = "cg"
+    kw.pop("inner_steps", None)
+    kw.pop("presteps", None)
+    fp64 = oracle.run_deck(decks.five_state_deck(72, **kw))
+    n = mixed.n_steps
+    assert all(r <= 1e-10 for r in mixed.relative_residual[:n])
+    if solver == "ppcg":
+        assert all(k > 0 for k in mixed.inner_iterations[:n])
+    a, b = mixed.summaries()[-1], fp64.summaries()[-1]
+    assert abs(a[5] - b[5]) <= 1e-8 * abs(b[5])
