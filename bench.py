@@ -52,7 +52,7 @@ WORKLOADS = {
 }
 
 
-ARITHMETIC = "fused"
+ARITHMETIC = "chain"  # set from --arithmetic in main()
 
 
 def deck_for(name, steps):
@@ -345,7 +345,7 @@ def run_kernels(args):
     name = args.workload
     cells, solver, prec, halo = WORKLOADS[name][:4]
     ch = lib.Chunk(cells, cells, halo, "ppcg", prec)
-    ch.set_arithmetic(ARITHMETIC == "fused")
+    ch.set_arithmetic(ARITHMETIC)
     decks.setup_five_state(ch, cells)
     ch.common_init(1, 0.004)
     ch.calc_residual()
@@ -694,6 +694,8 @@ def main():
     ap.add_argument("--lognormal", action="store_true",
                     help="--mode mixed: density times a seeded log-normal field")
     ap.add_argument("--reps", type=int, default=20)
+    ap.add_argument("--arithmetic", default="chain", choices=["exact", "fused", "chain"],
+                    help="arithmetic form of the FP64 kernels (tl_arithmetic)")
     ap.add_argument("--problems", type=int, default=512, help="--mode batch: problem count")
     ap.add_argument("--seed", type=int, default=0, help="--mode batch: problem seed")
     ap.add_argument("--directions", type=int, default=16,
@@ -706,6 +708,8 @@ def main():
     ap.add_argument("--sequential", type=int, default=32,
                     help="--mode batch: problems also run one by one for comparison")
     args = ap.parse_args()
+    global ARITHMETIC
+    ARITHMETIC = args.arithmetic
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
 

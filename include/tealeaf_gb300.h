@@ -200,10 +200,13 @@ int tea_gb300_configure(int halo_depth, int solver, int preconditioner,
  * expressions with each multiply feeding an add contracted into a fused
  * multiply-add, dot products accumulated with fused multiply-adds, and the
  * block-Jacobi strip's first division done with a stored reciprocal.
- * 0: every expression exactly as the reference writes it.  Applies to the
- * current chunk and to chunks created later; set it before
- * tea_leaf_common_init_kernel_ocl_.  Returns 0. */
-int tea_gb300_set_arithmetic(int fused);
+ * 0: every expression exactly as the reference writes it.  2: as 1, with
+ * the 5-point operator (and b - A x) as one left-to-right chain of fused
+ * multiply-adds, the fewest FP64 instructions.  Applies to the current
+ * chunk and to chunks, batches and adjoint objects created later; set it
+ * before tea_leaf_common_init_kernel_ocl_.  Returns 0, or -1 for another
+ * value. */
+int tea_gb300_set_arithmetic(int form);
 int tea_gb300_get_arithmetic(void);
 
 /* 1 (default): fatal errors abort; 0: record and return. */

@@ -144,8 +144,11 @@ class Chunk:
             raise RuntimeError("oracle_initialise failed %d" % rc)
         self.x_max, self.y_max, self.halo = x_max, y_max, halo
 
-    def set_arithmetic(self, fused):
-        lib().oracle_set_arithmetic(1 if fused else 0)
+    def set_arithmetic(self, form):
+        """0/False exact, 1/True fused, 2 chain (or the names)."""
+        if isinstance(form, str):
+            form = dict(exact=0, fused=1, chain=2)[form]
+        lib().oracle_set_arithmetic(int(form))
 
     # -- the same entry points as tealeaf_opencl_gb300.lib.Chunk -------------
     def initialise_chunk(self, xmin, ymin, dx, dy):

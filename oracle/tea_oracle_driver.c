@@ -45,7 +45,7 @@ typedef struct {
   int halo_depth;
   int test_problem;
   int verbose;
-  int fused; /* tl_arithmetic: 0 exact, 1 fused (default) */
+  int fused; /* tl_arithmetic: 0 exact, 1 fused (default), 2 chain */
   int mixed; /* tl_mixed_precision */
   double mixed_inner_eps;
   int mixed_max_outer;
@@ -266,10 +266,12 @@ static int parse_deck(const char* text, Deck* D, char* err, int errlen) {
         const char* v = next_word(&W);
         if (!strcmp(v, "exact")) D->fused = 0;
         else if (!strcmp(v, "fused")) D->fused = 1;
+        else if (!strcmp(v, "chain")) D->fused = 2;
         else {
           free(line);
           free_lines(&L);
-          return perr(err, errlen, "read_input: tl_arithmetic must be exact or fused");
+          return perr(err, errlen,
+                      "read_input: tl_arithmetic must be exact, fused or chain");
         }
       }
       else if (!strcmp(w, "tl_use_jacobi")) D->solver = ORC_SOLVER_JACOBI;

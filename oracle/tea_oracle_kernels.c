@@ -49,10 +49,13 @@ static int C_ready = 0;
  * reference kernels as written (each multiply and add rounded); 1 = the same
  * expressions with each multiply feeding an add contracted into one fused
  * multiply-add (C fma()), dot-product accumulation acc = fma(a,b,acc), and
- * the block-Jacobi first-row division done through a stored reciprocal. */
+ * the block-Jacobi first-row division done through a stored reciprocal;
+ * 2 = as 1, with the 5-point operator as one left-to-right chain of fma()
+ * (D x_c - Ky_n x_n - Ky_c x_s - Kx_e x_e - Kx_c x_w) and b - A x as the
+ * chain started from b. */
 static int FUSED = 1;
 
-void oracle_set_arithmetic(int fused) { FUSED = fused ? 1 : 0; }
+void oracle_set_arithmetic(int form) { FUSED = (form >= 0 && form <= 2) ? form : 1; }
 int oracle_get_arithmetic(void) { return FUSED; }
 
 #define IDX(col, row) ((long)(col) + (long)(row) * C.xs)
@@ -186,7 +189,7 @@ static double reduce_scratch(int k) {
 
 /* dot-product sum of scratch pairs (a in scratch, b in scratchb) */
 static double reduce_dot(int k) {
-  return reduce_pairs(C.scratch[k], C.scratchb[k], C.x_max, C.y_max, FUSED);
+  return reduce_pairs(C.scratch[k], C.scratchb[k], C.x_max, C.y_max, FUSED != 0);
 }
 
 #define SCR(k, col, row) \
@@ -362,9 +365,28 @@ static inline double smvp_at(const double* x, long c) {
   if (!FUSED)
     return D * x[c] - (C.Ky[c + xs] * x[c + xs] + C.Ky[c] * x[c - xs]) -
            (C.Kx[c + 1] * x[c + 1] + C.Kx[c] * x[c - 1]);
+  if (FUSED == 2) {
+    double t = D * x[c];
+    t = fma(-C.Ky[c + xs], x[c + xs], t);
+    t = fma(-C.Ky[c], x[c - xs], t);
+    t = fma(-C.Kx[c + 1], x[c + 1], t);
+    return fma(-C.Kx[c], x[c - 1], t);
+  }
   const double t1 = fma(C.Ky[c], x[c - xs], C.Ky[c + xs] * x[c + xs]);
   const double t2 = fma(C.Kx[c], x[c - 1], C.Kx[c + 1] * x[c + 1]);
   return fma(D, x[c], -t1) - t2;
+}
+
+/* b - A x: the reference's b - smvp, or the chain started from b */
+static inline double b_minus_smvp(const double* x, long c, double b) {
+  if (FUSED != 2) return b - smvp_at(x, c);
+  const long xs = C.xs;
+  const double D = (1.0 + (C.Ky[c + xs] + C.Ky[c]) + (C.Kx[c + 1] + C.Kx[c]));
+  double t = fma(-D, x[c], b);
+  t = fma(C.Ky[c + xs], x[c + xs], t);
+  t = fma(C.Ky[c], x[c - xs], t);
+  t = fma(C.Kx[c + 1], x[c + 1], t);
+  return fma(C.Kx[c], x[c - 1], t);
 }
 
 /* a*p + bl*br, the Chebyshev/PPCG coefficient update */
@@ -529,8 +551,7 @@ void oracle_calc_residual(void) {
   for (int row = H; row < H + C.y_max; row++)
     for (int col = H; col < H + C.x_max; col++) {
       const long c = IDX(col, row);
-      const double smvp = smvp_at(C.u, c);
-      C.r[c] = C.u0[c] - smvp;
+      C.r[c] = b_minus_smvp(C.u, c, C.u0[c]);
     }
 }
 
@@ -786,8 +807,7 @@ void oracle_ppcg_inner(int step) {
   for (int row = H; row < H + C.y_max; row++)
     for (int col = H; col < H + C.x_max; col++) {
       const long c = IDX(col, row);
-      const double result = smvp_at(C.sd, c);
-      C.r[c] = C.r[c] - result;
+      C.r[c] = b_minus_smvp(C.sd, c, C.r[c]);
     }
   double* zl = C.ztmp;
   if (C.prec == ORC_PREC_JAC_BLOCK) block_solve(C.r, zl);

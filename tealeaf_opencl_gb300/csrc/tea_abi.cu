@@ -248,7 +248,7 @@ static bool alloc_field(Chunk& c, Field& f) {
 struct Config {
   bool set = false;
   int halo = 1, solver = SOLVER_JACOBI, prec = PREC_NONE, profiler = 0;
-  int fused = 1;
+  int arith = 1;  // arithmetic form
 };
 static Config g_config;
 
@@ -322,7 +322,7 @@ static bool init_chunk(int x_max, int y_max, const Config& cfg) {
   c.solver = cfg.solver;
   c.prec = cfg.prec;
   c.profiler_on = cfg.profiler != 0;
-  c.fused = cfg.fused != 0;
+  c.arith = cfg.arith;
   c.TH = reduction_rows(x_max, y_max);
   c.S = ((long long)(x_max + 2 * c.H + 1 + 31) / 32) * 32;
   c.rows = y_max + 2 * c.H + 1;
@@ -734,13 +734,18 @@ extern "C" int tea_gb300_configure(int halo_depth, int solver,
 
 extern "C" void tea_gb300_set_abort_on_error(int a) { g_abort_on_error = a; }
 
-extern "C" int tea_gb300_set_arithmetic(int fused) {
-  g_config.fused = fused ? 1 : 0;
-  chunk().fused = fused != 0;
+extern "C" int tea_gb300_set_arithmetic(int form) {
+  if (form < 0 || form > 2) {
+    fail(3, "tea_gb300_set_arithmetic: form %d is not 0 (exact), 1 (fused) or 2 (chain)",
+         form);
+    return -1;
+  }
+  g_config.arith = form;
+  chunk().arith = form;
   return 0;
 }
 
-extern "C" int tea_gb300_get_arithmetic(void) { return chunk().fused ? 1 : 0; }
+extern "C" int tea_gb300_get_arithmetic(void) { return chunk().arith; }
 
 extern "C" int tea_gb300_last_error(char* msg, int len) {
   const int code = g_err_code;

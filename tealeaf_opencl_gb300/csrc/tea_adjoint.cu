@@ -112,7 +112,7 @@ struct Adjoint {
   bool ready = false;
   int x = 0, y = 0, coef = 1, prec = PREC_JAC_DIAG;
   double xmin = 0, xmax = 0, ymin = 0, ymax = 0;
-  bool fused = true;
+  int arith = 1;  // arithmetic form
   int num_sms = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -166,7 +166,7 @@ bool adj_ok(const char* who) {
   return true;
 }
 
-LaunchCtx ctx(const Adjoint& a) { return LaunchCtx{a.stream, a.num_sms, a.fused}; }
+LaunchCtx ctx(const Adjoint& a) { return LaunchCtx{a.stream, a.num_sms, a.arith}; }
 
 template <class K, class... Args>
 void launch_cells(const Adjoint& a, const char* name, K kernel, Args... args) {
@@ -265,7 +265,7 @@ extern "C" int tea_gb300_adjoint_create(int x_cells, int y_cells, double xmin,
   a.ymax = ymax;
   a.coef = coefficient;
   a.prec = preconditioner;
-  a.fused = tea_gb300_get_arithmetic() != 0;
+  a.arith = tea_gb300_get_arithmetic();
   int dev = 0;
   if (!check_cuda(cudaGetDevice(&dev), "cudaGetDevice")) return -1;
   cudaDeviceGetAttribute(&a.num_sms, cudaDevAttrMultiProcessorCount, dev);

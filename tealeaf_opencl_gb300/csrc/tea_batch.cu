@@ -106,7 +106,7 @@ __device__ __forceinline__ bool unit_done(unsigned int* counter, int units,
 
 // w = A p and p.w of every active problem (tea_leaf_cg_cl.cl:45-69); the
 // finishing block stores pw in the problem's loop state.
-template <bool F>
+template <int F>
 __global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
     k_b_calc_w(const Dev* __restrict__ devs, const Red* __restrict__ reds,
                ResState* st, WorkList wl) {
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
 
 // u, r, z updates and r.z (tea_leaf_cg_cl.cl:73-137) with alpha = rro/pw;
 // the finishing block takes the problem's scalar step and exit test.
-template <bool F>
+template <int F>
 __global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
     k_b_calc_ur(const Dev* __restrict__ devs, const Red* __restrict__ reds,
                 ResState* st, WorkList wl) {
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
 
 // p = z + beta p (tea_leaf_cg_cl.cl:141-160) for every problem whose
 // calc_ur has just run, including the iteration on which it stopped.
-template <bool F>
+template <int F>
 __global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
     k_b_calc_p(const Dev* __restrict__ devs, const Red* __restrict__ reds,
                ResState* st, WorkList wl) {
@@ -340,7 +340,7 @@ struct Batch {
   int n = 0;
   int prec = PREC_NONE, coef = 1;
   double xmin = 0, xmax = 0, ymin = 0, ymax = 0;
-  bool fused = true;
+  int arith = 1;  // arithmetic form
   int device = 0, num_sms = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t aux[kBranches] = {};
@@ -372,7 +372,7 @@ struct Batch {
   tea_gb300_batch_launch launch{0, 16, 1};
   int ustart_G = 0;             // G that ustart_all_d was built for
   int max_bps = 1;
-  int occ[2][3] = {};
+  int occ[3][3] = {};  // [arithmetic form][w, ur, p]
   cudaGraphExec_t iter_graph = nullptr;
   int graph_bps = 0, graph_iters = 0, graph_G = 0;
 };
@@ -433,17 +433,20 @@ int occupancy(const void* k) {
   return std::max(v, 1);
 }
 
-// Occupancy of the iteration kernels ([exact, fused][w, ur, p]) and the
+// Occupancy of the iteration kernels ([arithmetic form][w, ur, p]) and the
 // largest of them (the upper end of blocks_per_sm).
 int set_occupancy(Batch& b) {
-  b.occ[0][0] = occupancy((const void*)k_b_calc_w<false>);
-  b.occ[0][1] = occupancy((const void*)k_b_calc_ur<false>);
-  b.occ[0][2] = occupancy((const void*)k_b_calc_p<false>);
-  b.occ[1][0] = occupancy((const void*)k_b_calc_w<true>);
-  b.occ[1][1] = occupancy((const void*)k_b_calc_ur<true>);
-  b.occ[1][2] = occupancy((const void*)k_b_calc_p<true>);
+  b.occ[0][0] = occupancy((const void*)k_b_calc_w<0>);
+  b.occ[0][1] = occupancy((const void*)k_b_calc_ur<0>);
+  b.occ[0][2] = occupancy((const void*)k_b_calc_p<0>);
+  b.occ[1][0] = occupancy((const void*)k_b_calc_w<1>);
+  b.occ[1][1] = occupancy((const void*)k_b_calc_ur<1>);
+  b.occ[1][2] = occupancy((const void*)k_b_calc_p<1>);
+  b.occ[2][0] = occupancy((const void*)k_b_calc_w<2>);
+  b.occ[2][1] = occupancy((const void*)k_b_calc_ur<2>);
+  b.occ[2][2] = occupancy((const void*)k_b_calc_p<2>);
   int m = 1;
-  for (int f = 0; f < 2; f++)
+  for (int f = 0; f < 3; f++)
     for (int k = 0; k < 3; k++) m = std::max(m, b.occ[f][k]);
   return std::min(m, 8);
 }
@@ -489,7 +492,7 @@ extern "C" int tea_gb300_batch_create(int n, const int* x_cells, const int* y_ce
   b.xmax = xmax;
   b.ymin = ymin;
   b.ymax = ymax;
-  b.fused = tea_gb300_get_arithmetic() != 0;
+  b.arith = tea_gb300_get_arithmetic();
   if (!check_cuda(cudaGetDevice(&b.device), "cudaGetDevice")) return -1;
   cudaDeviceGetAttribute(&b.num_sms, cudaDevAttrMultiProcessorCount, b.device);
   b.ready = true;  // from here on release_batch frees partial allocations
@@ -614,7 +617,7 @@ extern "C" int tea_gb300_batch_create(int n, const int* x_cells, const int* y_ce
     return -1;
   }
   // cell volumes (initialise_chunk_kernel with dx, dy of each problem)
-  LaunchCtx l{b.stream, b.num_sms, b.fused};
+  LaunchCtx l{b.stream, b.num_sms, b.arith};
   for (int i = 0; i < n; i++) {
     const Problem& p = b.probs[i];
     const double dx = (xmax - xmin) / (double)(float)p.x;
@@ -731,7 +734,7 @@ void for_each_problem(Batch& b, F f) {
   for (int k = 0; k < kBranches; k++) cudaStreamWaitEvent(b.aux[k], b.fork, 0);
   for (int j = 0; j < b.n; j++) {
     const int i = b.order[j];
-    const LaunchCtx l{b.aux[j % kBranches], b.num_sms, b.fused};
+    const LaunchCtx l{b.aux[j % kBranches], b.num_sms, b.arith};
     f(l, b.probs[i]);
   }
   for (int k = 0; k < kBranches; k++) {
@@ -792,9 +795,9 @@ WorkList work_list(const Batch& b) {
 // number of kernels queued.
 // One CG iteration; each kernel's grid is bps blocks per SM, capped by
 // that kernel's own occupancy (b.occ).
-template <bool F>
+template <int F>
 void enqueue_iteration(Batch& b, const WorkList& wl, int bps) {
-  const int* occ = b.occ[F ? 1 : 0];
+  const int* occ = b.occ[F];
   auto grid = [&](int k) { return std::max(1, b.num_sms * std::min(bps, occ[k])); };
   k_b_calc_w<F><<<grid(0), kBlock, 0, b.stream>>>(b.devs_d, b.reds_d, b.st_d, wl);
   k_b_calc_ur<F><<<grid(1), kBlock, 0, b.stream>>>(b.devs_d, b.reds_d, b.st_d, wl);
@@ -804,10 +807,12 @@ void enqueue_iteration(Batch& b, const WorkList& wl, int bps) {
 int enqueue_iterations(Batch& b, int iters, int bps, bool compact) {
   const WorkList wl = work_list(b);
   for (int k = 0; k < iters; k++) {
-    if (b.fused)
-      enqueue_iteration<true>(b, wl, bps);
+    if (b.arith == 2)
+      enqueue_iteration<2>(b, wl, bps);
+    else if (b.arith == 1)
+      enqueue_iteration<1>(b, wl, bps);
     else
-      enqueue_iteration<false>(b, wl, bps);
+      enqueue_iteration<0>(b, wl, bps);
   }
   int launched = 3 * iters;
   if (compact) {

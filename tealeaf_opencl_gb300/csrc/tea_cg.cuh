@@ -15,7 +15,7 @@ namespace tea {
 // the order of the per-lane sums are those of the row-by-row form.
 
 // w = A p and the lane's share of p.w (tea_leaf_cg_cl.cl:45-69)
-template <int TH, bool F>
+template <int TH, int F>
 __device__ __forceinline__ void cg_w_tile(const Dev& d, int x, int y0, bool xin,
                                           double* acc) {
 #pragma unroll 1
@@ -40,7 +40,7 @@ __device__ __forceinline__ void cg_w_tile(const Dev& d, int x, int y0, bool xin,
 }
 
 // u += alpha p; r -= alpha w (tea_leaf_cg_cl.cl:88-89) on loaded values
-template <bool F>
+template <int F>
 __device__ __forceinline__ void ur_values(double alpha, double& u, double p,
                                           double& r, double w) {
   if (F) {
@@ -54,7 +54,7 @@ __device__ __forceinline__ void ur_values(double alpha, double& u, double p,
 
 // u += alpha p, r -= alpha w, z = M^-1 r and the lane's share of r.z (and
 // of r.r when NV == 2), tea_leaf_cg_cl.cl:73-137
-template <int TH, bool F, int NV>
+template <int TH, int F, int NV>
 __device__ __forceinline__ void cg_ur_tile(const Dev& d, int x, int y0, bool xin,
                                            double* acc, double alpha) {
 #pragma unroll 1
@@ -108,7 +108,7 @@ __device__ __forceinline__ void cg_ur_tile(const Dev& d, int x, int y0, bool xin
 
 // p = z + beta p, or r + beta p without a preconditioner
 // (tea_leaf_cg_cl.cl:141-160)
-template <int TH, bool F>
+template <int TH, int F>
 __device__ __forceinline__ void cg_p_tile(const Dev& d, int x, int y0, bool xin,
                                           double beta) {
   if (!xin) return;

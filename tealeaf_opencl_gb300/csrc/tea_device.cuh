@@ -20,14 +20,21 @@
 // All arithmetic is compiled with --fmad=false, so every operation rounds
 // exactly as written.
 //
-// Two arithmetic forms, chosen per chunk (template parameter F):
-//   exact (F = false): every expression of the reference kernels as written,
+// Three arithmetic forms, chosen per chunk (template parameter F):
+//   exact (F = 0): every expression of the reference kernels as written,
 //     each multiply and add rounded separately;
-//   fused (F = true): the same expressions with each multiply feeding an add
+//   fused (F = 1): the same expressions with each multiply feeding an add
 //     contracted into one fused multiply-add (what OpenCL's default
 //     FP_CONTRACT allows a GPU compiler to do), and the per-strip division of
 //     the block-Jacobi solve replaced by a multiply with the reciprocal kept
-//     in bfp at the strip's first row.
+//     in bfp at the strip's first row;
+//   chain (F = 2): fused, except that the 5-point operator is one chain of
+//     fused multiply-adds, A x = D x_c - Ky_n x_n - Ky_c x_s - Kx_e x_e -
+//     Kx_c x_w evaluated left to right, and b - A x starts the chain from b.
+//     That re-associates the reference's expression (no compiler contraction
+//     does that), for the fewest FP64 instructions: 5 per operator
+//     application against 6 (fused) and 9 (exact), and 5 per b - A x
+//     against 7 and 10.
 // The diagonal 1 + (Ky_n + Ky_c) + (Kx_e + Kx_c) is precomputed once per
 // timestep into d.diag with the reference's association, so using it is
 // bit-identical to recomputing it.  GB300's FP64 pipe, not HBM, bounds these
@@ -54,7 +61,7 @@ __device__ __forceinline__ double bfly(double v) {
 // (e.g. tea_leaf_cg_cl.cl:59-63):
 //   (1 + (Ky_n + Ky_c) + (Kx_e + Kx_c)) x_c - (Ky_n x_n + Ky_c x_s)
 //                                           - (Kx_e x_e + Kx_c x_w)
-template <bool F>
+template <int F>
 __device__ __forceinline__ double smvp(const Dev& d, const double* x,
                                        long long c) {
   const long long S = d.S;
@@ -64,13 +71,35 @@ __device__ __forceinline__ double smvp(const Dev& d, const double* x,
   if (!F)
     return D * x[c] - (kyn * x[c + S] + kyc * x[c - S]) -
            (kxe * x[c + 1] + kxc * x[c - 1]);
+  if (F == 2) {
+    double t = D * x[c];
+    t = __fma_rn(-kyn, x[c + S], t);
+    t = __fma_rn(-kyc, x[c - S], t);
+    t = __fma_rn(-kxe, x[c + 1], t);
+    return __fma_rn(-kxc, x[c - 1], t);
+  }
   const double t1 = __fma_rn(kyc, x[c - S], kyn * x[c + S]);
   const double t2 = __fma_rn(kxc, x[c - 1], kxe * x[c + 1]);
   return __fma_rn(D, x[c], -t1) - t2;
 }
 
+// b - A x at offset c: the reference's "b - smvp" (calc_residual,
+// tea_leaf_common_cl.cl:17-36; ppcg update_r, tea_leaf_ppcg_cl.cl:62-88),
+// or in the chain form the chain of fused multiply-adds started from b.
+template <int F>
+__device__ __forceinline__ double b_minus_smvp(const Dev& d, const double* x,
+                                               long long c, double b) {
+  if (F != 2) return b - smvp<F>(d, x, c);
+  const long long S = d.S;
+  double t = __fma_rn(-__ldg(d.diag + c), x[c], b);
+  t = __fma_rn(__ldg(d.Ky + c + S), x[c + S], t);
+  t = __fma_rn(__ldg(d.Ky + c), x[c - S], t);
+  t = __fma_rn(__ldg(d.Kx + c + 1), x[c + 1], t);
+  return __fma_rn(__ldg(d.Kx + c), x[c - 1], t);
+}
+
 // acc + a*b of the per-lane dot-product accumulation
-template <bool F>
+template <int F>
 __device__ __forceinline__ double accum(double acc, double a, double b) {
   return F ? __fma_rn(a, b, acc) : acc + a * b;
 }
@@ -92,21 +121,21 @@ __device__ __forceinline__ int strip_rows(const Dev& d, int y) {
 
 // One forward step of the strip's Thomas algorithm:
 // (r - COEF_A dp) * bfp with COEF_A = -Ky
-template <bool F>
+template <int F>
 __device__ __forceinline__ double fwd(double r, double ky, double dp,
                                       double bfp) {
   return F ? __fma_rn(ky, dp, r) * bfp : (r - (-ky) * dp) * bfp;
 }
 
 // One back-substitution step: dp - cp z
-template <bool F>
+template <int F>
 __device__ __forceinline__ double bwd(double dp, double cp, double z) {
   return F ? __fma_rn(-cp, z, dp) : dp - cp * z;
 }
 
 // block_solve_func (tea_block_jacobi.cl:6-42) for one column of one strip:
 // z = M_block^-1 r for the strip whose first cell is at offset c0.
-template <bool F>
+template <int F>
 __device__ __forceinline__ void strip_solve(const Dev& d, long long c0,
                                             int upper, const double rl[4],
                                             double zl[4]) {

@@ -56,7 +56,7 @@ struct Deck {
   int halo = 1;
   int test_problem = 0;
   bool verbose = false;
-  bool fused = true;  // tl_arithmetic
+  int arith = 1;  // tl_arithmetic: 0 exact, 1 fused, 2 chain
   bool mixed = false;        // tl_mixed_precision
   bool true_exit = false;    // tl_exit_true_residual (resident CG only)
   double mixed_inner_eps = 1e-4;
@@ -182,10 +182,11 @@ bool parse_deck(const std::string& text, Deck* D, std::string* err) {
       else if (w == "tl_arithmetic") {
         // not a reference key: the arithmetic form of the solver kernels
         const std::string v = next();
-        if (v == "exact") D->fused = false;
-        else if (v == "fused") D->fused = true;
+        if (v == "exact") D->arith = 0;
+        else if (v == "fused") D->arith = 1;
+        else if (v == "chain") D->arith = 2;
         else {
-          *err = "read_input: tl_arithmetic must be exact or fused";
+          *err = "read_input: tl_arithmetic must be exact, fused or chain";
           return false;
         }
       }
@@ -423,7 +424,7 @@ class Driver {
     mode = m;
     cap = c;
     if (log_path) logfile = fopen(log_path, "w");
-    tea_gb300_set_arithmetic(D.fused ? 1 : 0);
+    tea_gb300_set_arithmetic(D.arith);
     if (tea_gb300_configure(D.halo, D.solver, D.prec, 0) != 0) {
       *err = "invalid configuration";
       return false;

@@ -86,7 +86,7 @@ struct Chunk {
   cudaStream_t stream = nullptr;
   Field density, energy0, energy1, volume, u, u0, p, r, w, Mi, Kx, Ky, sd, z,
       cp, bfp, diag;
-  bool fused = true;  // arithmetic form (see tea_device.cuh)
+  int arith = 1;  // arithmetic form: 0 exact, 1 fused, 2 chain (tea_device.cuh)
   double *cellx = nullptr, *celly = nullptr, *celldx = nullptr,
          *celldy = nullptr, *vertexx = nullptr, *vertexy = nullptr,
          *vertexdx = nullptr, *vertexdy = nullptr;
@@ -174,7 +174,7 @@ void launch_update_halo(Chunk& c, int mask, int depth);
 struct LaunchCtx {
   cudaStream_t stream;
   int num_sms;
-  bool fused;
+  int arith;  // arithmetic form
 };
 Dev make_dev_tiling(Dev d);  // fills th, ntx, nsx, nty, ns from x_max, y_max
 void dev_volume(const LaunchCtx& l, const Dev& d, double vol);

@@ -53,19 +53,23 @@ static void launch_2d(Chunk& c, const char* name, int nx, int ny,
   profile_end(name);
 }
 
-#define TH_DISPATCH(c, name, kern, ...)                       \
-  do {                                                        \
-    if ((c).TH == 16) {                                       \
-      if ((c).fused)                                          \
-        launch_tile(c, name, kern<16, true>, __VA_ARGS__);    \
-      else                                                    \
-        launch_tile(c, name, kern<16, false>, __VA_ARGS__);   \
-    } else {                                                  \
-      if ((c).fused)                                          \
-        launch_tile(c, name, kern<4, true>, __VA_ARGS__);     \
-      else                                                    \
-        launch_tile(c, name, kern<4, false>, __VA_ARGS__);    \
-    }                                                         \
+#define TH_DISPATCH(c, name, kern, ...)                  \
+  do {                                                   \
+    if ((c).TH == 16) {                                  \
+      if ((c).arith == 2)                                \
+        launch_tile(c, name, kern<16, 2>, __VA_ARGS__);  \
+      else if ((c).arith == 1)                           \
+        launch_tile(c, name, kern<16, 1>, __VA_ARGS__);  \
+      else                                               \
+        launch_tile(c, name, kern<16, 0>, __VA_ARGS__);  \
+    } else {                                             \
+      if ((c).arith == 2)                                \
+        launch_tile(c, name, kern<4, 2>, __VA_ARGS__);   \
+      else if ((c).arith == 1)                           \
+        launch_tile(c, name, kern<4, 1>, __VA_ARGS__);   \
+      else                                               \
+        launch_tile(c, name, kern<4, 0>, __VA_ARGS__);   \
+    }                                                    \
   } while (0)
 
 // ---------------------------------------------------------------------------
@@ -277,7 +281,7 @@ __global__ void k_update_halo(Dev d, int mask, int depth) {
 // ---------------------------------------------------------------------------
 
 // tea_leaf_calc_residual, tea_leaf_common_cl.cl:17-36
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock) k_calc_residual(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
@@ -289,8 +293,7 @@ __global__ void __launch_bounds__(kBlock) k_calc_residual(Dev d, Red red) {
       for (int j = 0; j < 4; j++)
         if (g + j < d.y_max) {
           const long long c = c0 + j * d.S;
-          const double s = smvp<F>(d, d.u, c);
-          rv[j] = d.u0[c] - s;
+          rv[j] = b_minus_smvp<F>(d, d.u, c, d.u0[c]);
         }
 #pragma unroll
       for (int j = 0; j < 4; j++)
@@ -300,7 +303,7 @@ __global__ void __launch_bounds__(kBlock) k_calc_residual(Dev d, Red red) {
 }
 
 // tea_leaf_calc_2norm, tea_leaf_common_cl.cl:38-54
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock)
     k_dot(Dev d, Red red, const double* a, const double* b) {
   tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
@@ -321,7 +324,7 @@ __global__ void __launch_bounds__(kBlock)
 // tea_leaf_block_solve (tea_block_jacobi.cl:44-76) fused with
 // tea_leaf_cg_solve_init_p (tea_leaf_cg_cl.cl:8-41): z = M^-1 r, p = z,
 // sum r.p
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock) k_cg_init_p(Dev d, Red red) {
   tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (d.prec == PREC_JAC_BLOCK) {
@@ -377,7 +380,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_init_p(Dev d, Red red) {
 // tea_leaf_cg_solve_calc_w, tea_leaf_cg_cl.cl:45-69.  With st != nullptr
 // (device-resident loop) it does nothing once the loop has stopped and
 // leaves pw in st.
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock)
     k_cg_calc_w(Dev d, Red red, ResState* st) {
   if (st && *(volatile int*)&st->stop) return;
@@ -392,7 +395,7 @@ __global__ void __launch_bounds__(kBlock)
 // finishes the reduction carries out the host steps of one CG iteration
 // (cg_scalar_step).  With NV = 2 it also sums r.r, for the resident loop's
 // optional exit test on the unpreconditioned residual.
-template <int TH, bool F, int NV = 1>
+template <int TH, int F, int NV = 1>
 __global__ void __launch_bounds__(kBlock)
     k_cg_calc_ur(Dev d, Red red, double alpha, ResState* st) {
   if (st) {
@@ -411,7 +414,7 @@ __global__ void __launch_bounds__(kBlock)
 // tea_leaf_cg_solve_calc_p, tea_leaf_cg_cl.cl:141-160.  In the
 // device-resident loop it runs once per calc_ur that ran, with that
 // iteration's beta.
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock)
     k_cg_calc_p(Dev d, Red red, double beta, ResState* st,
                 unsigned int* counter) {
@@ -432,7 +435,7 @@ __global__ void __launch_bounds__(kBlock)
 // alpha p + beta M^-1 r of tea_leaf_cheby_cl.cl:134-144 and
 // tea_leaf_ppcg_cl.cl:137-152, with bl br = beta z, (beta Mi) r, beta r or
 // (beta r) Mi as each reference expression groups it
-template <bool F>
+template <int F>
 __device__ __forceinline__ double cheby_update(double a, double p, double bl,
                                                double br) {
   return F ? __fma_rn(a, p, bl * br) : a * p + bl * br;
@@ -442,7 +445,7 @@ __device__ __forceinline__ double cheby_update(double a, double p, double bl,
 // tea_leaf_cheby_solve_calc_p (tea_leaf_cheby_cl.cl:4-64, :78-145):
 // w = A u, r = u0 - w, then p from M^-1 r.  mode 0: p = M^-1 r / theta;
 // mode 1: p = alpha p + beta M^-1 r.
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock)
     k_cheby_p(Dev d, Red red, int mode, double theta, double alpha,
               double beta) {
@@ -522,7 +525,7 @@ __global__ void __launch_bounds__(kBlock)
 }
 
 // tea_leaf_cheby_solve_calc_u, tea_leaf_cheby_cl.cl:66-76
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock) k_cheby_calc_u(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
@@ -547,7 +550,7 @@ __global__ void __launch_bounds__(kBlock) k_cheby_calc_u(Dev d, Red red) {
 // (tea_leaf_ppcg_cl.cl:4-60, mode 0: sd = M^-1 r / theta) and
 // tea_leaf_ppcg_solve_calc_sd (:90-155, mode 1: sd = alpha sd + beta M^-1 r,
 // diagonal case alpha sd + (beta r) Mi)
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock)
     k_ppcg_sd(Dev d, Red red, int mode, double theta, double alpha,
               double beta) {
@@ -609,7 +612,7 @@ __global__ void __launch_bounds__(kBlock)
 }
 
 // tea_leaf_ppcg_solve_update_r, tea_leaf_ppcg_cl.cl:62-88
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock) k_ppcg_update_r(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
@@ -622,8 +625,7 @@ __global__ void __launch_bounds__(kBlock) k_ppcg_update_r(Dev d, Red red) {
         if (g + j < d.y_max) {
           const long long c = c0 + j * d.S;
           uv[j] = d.u[c] + d.sd[c];
-          const double result = smvp<F>(d, d.sd, c);
-          rv[j] = d.r[c] - result;
+          rv[j] = b_minus_smvp<F>(d, d.sd, c, d.r[c]);
         }
 #pragma unroll
       for (int j = 0; j < 4; j++)
@@ -637,7 +639,7 @@ __global__ void __launch_bounds__(kBlock) k_ppcg_update_r(Dev d, Red red) {
 
 // tea_leaf_jacobi_copy_u, tea_leaf_jacobi_cl.cl:3-13 (un is vector_Mi, as
 // in the reference, ocl_kernels.cpp:576-585)
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock) k_jacobi_copy_u(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
@@ -657,7 +659,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_copy_u(Dev d, Red red) {
 
 // tea_leaf_jacobi_solve, tea_leaf_jacobi_cl.cl:15-42 (the same arithmetic in
 // both forms; its denominator associates differently from the diagonal)
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock) k_jacobi_solve(Dev d, Red red) {
   tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
     const long long S = d.S;
@@ -688,7 +690,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_solve(Dev d, Red red) {
 }
 
 // tea_leaf_finalise, tea_leaf_common_cl.cl:4-15
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock) k_finalise(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
@@ -708,7 +710,7 @@ __global__ void __launch_bounds__(kBlock) k_finalise(Dev d, Red red) {
 
 // field_summary, field_summary_cl.cl:3-43 (energy argument bound to energy1,
 // ocl_kernels.cpp:466-469); the same arithmetic in both forms
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock) k_field_summary(Dev d, Red red) {
   tile_driver<TH, 4>(d, red, [&](int x, int y0, bool xin, double* acc) {
 #pragma unroll 2
@@ -734,7 +736,7 @@ __global__ void __launch_bounds__(kBlock) k_field_summary(Dev d, Red red) {
 
 // The diagonal 1 + (Ky_n + Ky_c) + (Kx_e + Kx_c) of every interior cell, in
 // the association of the reference's inline expression
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock) k_init_diag(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
@@ -821,7 +823,7 @@ void launch_init_jac_diag(Chunk& c) {
 void launch_block_init(Chunk& c) {
   const Dev d = c.dev();
   launch_2d(c, "tea_leaf_block_init", d.x_max, (d.y_max + 3) / 4, k_block_init, d,
-            c.fused ? 1 : 0);
+            c.arith != 0 ? 1 : 0);
 }
 
 void launch_cg_init_p(Chunk& c) {
@@ -931,19 +933,23 @@ static void ctx_2d(const LaunchCtx& l, const char* name, int nx, int ny,
   check_cuda(cudaGetLastError(), name);
 }
 
-#define CTX_DISPATCH(l, d, name, kern, ...)                       \
-  do {                                                            \
-    if ((d).th == 16) {                                           \
-      if ((l).fused)                                              \
-        ctx_tile(l, d, name, kern<16, true>, __VA_ARGS__);        \
-      else                                                        \
-        ctx_tile(l, d, name, kern<16, false>, __VA_ARGS__);       \
-    } else {                                                      \
-      if ((l).fused)                                              \
-        ctx_tile(l, d, name, kern<4, true>, __VA_ARGS__);         \
-      else                                                        \
-        ctx_tile(l, d, name, kern<4, false>, __VA_ARGS__);        \
-    }                                                             \
+#define CTX_DISPATCH(l, d, name, kern, ...)              \
+  do {                                                   \
+    if ((d).th == 16) {                                  \
+      if ((l).arith == 2)                                \
+        ctx_tile(l, d, name, kern<16, 2>, __VA_ARGS__);  \
+      else if ((l).arith == 1)                           \
+        ctx_tile(l, d, name, kern<16, 1>, __VA_ARGS__);  \
+      else                                               \
+        ctx_tile(l, d, name, kern<16, 0>, __VA_ARGS__);  \
+    } else {                                             \
+      if ((l).arith == 2)                                \
+        ctx_tile(l, d, name, kern<4, 2>, __VA_ARGS__);   \
+      else if ((l).arith == 1)                           \
+        ctx_tile(l, d, name, kern<4, 1>, __VA_ARGS__);   \
+      else                                               \
+        ctx_tile(l, d, name, kern<4, 0>, __VA_ARGS__);   \
+    }                                                    \
   } while (0)
 
 void dev_volume(const LaunchCtx& l, const Dev& d, double vol) {
@@ -975,7 +981,7 @@ void dev_dot(const LaunchCtx& l, const Dev& d, const Red& r, const double* a,
 }
 void dev_block_init(const LaunchCtx& l, const Dev& d) {
   ctx_2d(l, "tea_leaf_block_init", d.x_max, (d.y_max + 3) / 4, k_block_init, d,
-         l.fused ? 1 : 0);
+         l.arith != 0 ? 1 : 0);
 }
 void dev_update_halo(const LaunchCtx& l, const Dev& d, int mask, int depth) {
   if (!mask || depth < 1) return;
@@ -1010,7 +1016,7 @@ static int tile_grid(Chunk& c, void (*kernel)(KArgs...)) {
   return (int)std::max<long long>(1, std::min<long long>(c.dev().ns, cap));
 }
 
-template <int TH, bool F, int NV>
+template <int TH, int F, int NV>
 static void enqueue_resident_iterations_t(Chunk& c, int iters) {
   const Dev d = c.dev();
   const Red red = c.red();
@@ -1025,14 +1031,22 @@ static void enqueue_resident_iterations_t(Chunk& c, int iters) {
   }
 }
 
+template <int TH, int NV>
+static void enqueue_resident_iterations_th(Chunk& c, int iters) {
+  if (c.arith == 2)
+    enqueue_resident_iterations_t<TH, 2, NV>(c, iters);
+  else if (c.arith == 1)
+    enqueue_resident_iterations_t<TH, 1, NV>(c, iters);
+  else
+    enqueue_resident_iterations_t<TH, 0, NV>(c, iters);
+}
+
 template <int NV>
 static void enqueue_resident_iterations_nv(Chunk& c, int iters) {
   if (c.TH == 16)
-    c.fused ? enqueue_resident_iterations_t<16, true, NV>(c, iters)
-            : enqueue_resident_iterations_t<16, false, NV>(c, iters);
+    enqueue_resident_iterations_th<16, NV>(c, iters);
   else
-    c.fused ? enqueue_resident_iterations_t<4, true, NV>(c, iters)
-            : enqueue_resident_iterations_t<4, false, NV>(c, iters);
+    enqueue_resident_iterations_th<4, NV>(c, iters);
 }
 
 static void enqueue_resident_iterations(Chunk& c, int iters, bool true_exit) {

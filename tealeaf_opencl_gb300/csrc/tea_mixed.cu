@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(kBlock)
         r32[j] = z[j] = 0.0f;
         if (xin && g + j < d.y_max) {
           const long long c = cidx(d, x, g + j);
-          r64[j] = d.u0[c] - smvp<true>(d, d.u, c);
+          r64[j] = d.u0[c] - smvp<1>(d, d.u, c);
           r32[j] = (float)r64[j];
           z[j] = m.Mi[cidx32(d, m, x, g + j)] * r32[j];
         }

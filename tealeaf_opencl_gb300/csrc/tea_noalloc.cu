@@ -29,7 +29,7 @@ constexpr long long kNoAllocMaxPartials = 65536;
 // counter in the element after them.  Shared by every call on a device.
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxPartials + 32];
 
-template <int TH, bool F>
+template <int TH, int F>
 __global__ void __launch_bounds__(kBlock)
     k_dot_noalloc(Dev d, Red red, const double* a, const double* b) {
   tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
@@ -69,7 +69,7 @@ static double* scratch_for_current_device() {
   return g_scratch_addr[dev];
 }
 
-template <int TH, bool F>
+template <int TH, int F>
 static int launch_dot_noalloc(const Dev& d, const Red& red, const double* a,
                               const double* b, cudaStream_t s) {
   int dev = 0, sms = 0, per_sm = 0;
@@ -134,8 +134,8 @@ extern "C" int tea_gb300_dot_noalloc(const double* a, const double* b,
   red.result = result;
   const bool fused = tea_gb300_get_arithmetic() != 0;
   if (TH == 16)
-    return fused ? launch_dot_noalloc<16, true>(d, red, a, b, s)
-                 : launch_dot_noalloc<16, false>(d, red, a, b, s);
-  return fused ? launch_dot_noalloc<4, true>(d, red, a, b, s)
-               : launch_dot_noalloc<4, false>(d, red, a, b, s);
+    return fused ? launch_dot_noalloc<16, 1>(d, red, a, b, s)
+                 : launch_dot_noalloc<16, 0>(d, red, a, b, s);
+  return fused ? launch_dot_noalloc<4, 1>(d, red, a, b, s)
+               : launch_dot_noalloc<4, 0>(d, red, a, b, s);
 }

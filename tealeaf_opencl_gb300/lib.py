@@ -76,6 +76,16 @@ class MixedInfo(C.Structure):
     ]
 
 
+ARITHMETIC = dict(exact=0, fused=1, chain=2)
+
+
+def arithmetic_form(form):
+    """Arithmetic form number from a name, a bool (fused or not) or a number."""
+    if isinstance(form, str):
+        return ARITHMETIC[form]
+    return int(form)
+
+
 class BatchStats(C.Structure):
     _fields_ = [
         ("steps", C.c_int), ("max_iterations", C.c_int), ("iterations", C.c_longlong),
@@ -253,8 +263,9 @@ class Chunk:
         self.x_max, self.y_max, self.halo = x_max, y_max, halo
         self.neighbours = np.full(4, EXTERNAL_FACE, dtype=np.int32)
 
-    def set_arithmetic(self, fused):
-        load().tea_gb300_set_arithmetic(1 if fused else 0)
+    def set_arithmetic(self, form):
+        """0/False exact, 1/True fused, 2 chain (or the names)."""
+        load().tea_gb300_set_arithmetic(arithmetic_form(form))
 
     # -- setup -------------------------------------------------------------
     def initialise_chunk(self, xmin, ymin, dx, dy):

@@ -43,7 +43,7 @@ def single_chunk(problem, prec, mode, steps=STEPS, eps=EPS, max_iters=5000):
 
 
 def make_batch(problems, fields, prec, mode):
-    lib.load().tea_gb300_set_arithmetic(1 if mode == "fused" else 0)
+    lib.load().tea_gb300_set_arithmetic(lib.arithmetic_form(mode))
     b = lib.Batch([(p["x"], p["y"]) for p in problems], prec=prec)
     for i, (d, e) in enumerate(fields):
         b.set_fields(i, d, e)
@@ -64,7 +64,8 @@ def problem_set():
 
 
 @pytest.mark.parametrize("prec,mode", [("jac_diag", "fused"), ("jac_diag", "exact"),
-                                       ("none", "fused"), ("jac_block", "fused")])
+                                       ("jac_diag", "chain"), ("none", "fused"),
+                                       ("jac_block", "fused")])
 def test_batch_matches_single_chunk_runs(prec, mode):
     problems = problem_set()
     ref = [single_chunk(p, prec, mode) for p in problems]

@@ -53,7 +53,7 @@ CASES = [
 ]
 
 
-@pytest.mark.parametrize("fused", [True, False], ids=["fused", "exact"])
+@pytest.mark.parametrize("fused", [1, 0, 2], ids=["fused", "exact", "chain"])
 @pytest.mark.parametrize("x,y,H,solver,prec,kw", CASES,
                          ids=["%dx%d-h%d-%s-%s%s" % (c[0], c[1], c[2], c[3], c[4],
                                                       "-" + "-".join(sorted(c[5])) if c[5] else "")
@@ -64,7 +64,7 @@ def test_entry_points_bit_exact(x, y, H, solver, prec, kw, fused):
     assert not bad, bad
 
 
-@pytest.mark.parametrize("fused", [True, False], ids=["fused", "exact"])
+@pytest.mark.parametrize("fused", [1, 0, 2], ids=["fused", "exact", "chain"])
 def test_tall_tiles_bit_exact(fused):
     """A grid large enough for 16-row reduction tiles."""
     from tealeaf_opencl_gb300 import lib

@@ -49,7 +49,7 @@ def assert_matches_oracle(steps, res):
     assert (last.vol, last.mass, last.ie, last.temp) == tuple(final[[1, 2, 4, 5]])
 
 
-@pytest.mark.parametrize("mode", ["exact", "fused"])
+@pytest.mark.parametrize("mode", ["exact", "fused", "chain"])
 @pytest.mark.parametrize("tp", [1, 6])
 def test_test_problem_matches_golden_and_oracle(tp, mode):
     deck, temp = problem(tp)
@@ -81,7 +81,7 @@ def test_long_cg_test_problems_match_golden(tp):
     assert steps[-1].qa_passed == 1, steps[-1].qa_diff
 
 
-@pytest.mark.parametrize("mode", ["exact", "fused"])
+@pytest.mark.parametrize("mode", ["exact", "fused", "chain"])
 def test_c1_512_cg_jac_diag_matches_oracle(mode):
     """512x512 CG + diagonal Jacobi, eps 1e-15, 10 steps."""
     deck = decks.five_state_deck(512, solver="cg", prec="jac_diag", steps=10,
@@ -96,9 +96,11 @@ def test_c1_512_cg_jac_diag_matches_oracle(mode):
 
 @pytest.mark.parametrize("solver,prec", [("chebyshev", "jac_block"), ("ppcg", "jac_block"),
                                          ("chebyshev", "jac_diag"), ("ppcg", "none")])
-def test_cheby_ppcg_decks_match_oracle(solver, prec):
+@pytest.mark.parametrize("mode", ["fused", "chain"])
+def test_cheby_ppcg_decks_match_oracle(solver, prec, mode):
     deck = decks.five_state_deck(256, solver=solver, prec=prec, steps=4, eps=1e-15,
-                                 max_iters=5000, halo=2, inner_steps=10, presteps=20)
+                                 max_iters=5000, halo=2, inner_steps=10, presteps=20,
+                                 extra="tl_arithmetic %s" % mode)
     assert_matches_oracle(gpu_run(deck), oracle.run_deck(deck))
 
 

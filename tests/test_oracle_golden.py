@@ -31,7 +31,7 @@ def check(tp, mode="fused"):
     return res
 
 
-@pytest.mark.parametrize("mode", ["exact", "fused"])
+@pytest.mark.parametrize("mode", ["exact", "fused", "chain"])
 def test_tp1_jacobi_10x10(mode):
     res = check(1, mode)
     assert res.n_steps == 10
@@ -39,7 +39,7 @@ def test_tp1_jacobi_10x10(mode):
     assert all(0 < res.iterations[i] < 1000 for i in range(10))
 
 
-@pytest.mark.parametrize("mode", ["exact", "fused"])
+@pytest.mark.parametrize("mode", ["exact", "fused", "chain"])
 def test_tp6_ppcg_500x500_halo4(mode):
     res = check(6, mode)
     assert res.n_steps == 20
@@ -50,7 +50,7 @@ def test_tp6_ppcg_500x500_halo4(mode):
 
 
 @pytest.mark.slow
-@pytest.mark.parametrize("mode", ["exact", "fused"])
+@pytest.mark.parametrize("mode", ["exact", "fused", "chain"])
 def test_tp2_cg_960x960(mode):
     check(2, mode)
 
@@ -60,16 +60,21 @@ def test_tp3_cg_3840x3840():
     check(3)
 
 
-def test_arithmetic_forms_agree_within_tolerance():
-    """The fused and exact forms differ only by rounding: on a 64^2 CG run
-    the field summaries agree to 1e-12 and the iteration counts to 1."""
+@pytest.mark.parametrize("other", ["fused", "chain"])
+@pytest.mark.parametrize("solver,prec", [("cg", "jac_diag"), ("ppcg", "jac_block")])
+def test_arithmetic_forms_agree_within_tolerance(other, solver, prec):
+    """The fused and chain forms differ from the exact one only by rounding:
+    on a 64^2 run the field summaries agree to 1e-12 and the iteration
+    counts to 1."""
     from tealeaf_opencl_gb300 import decks
     out = {}
-    for mode in ("exact", "fused"):
-        deck = decks.five_state_deck(64, solver="cg", prec="jac_diag", steps=5,
-                                     eps=1e-15, extra="tl_arithmetic %s" % mode)
+    for mode in ("exact", other):
+        deck = decks.five_state_deck(64, solver=solver, prec=prec, steps=5, eps=1e-15,
+                                     inner_steps=8 if solver == "ppcg" else None,
+                                     presteps=20 if solver == "ppcg" else None,
+                                     extra="tl_arithmetic %s" % mode)
         out[mode] = oracle.run_deck(deck)
-    a, b = out["exact"], out["fused"]
+    a, b = out["exact"], out[other]
     sa, sb = a.summaries()[-1], b.summaries()[-1]
     assert max(abs(sa[i] - sb[i]) / abs(sa[i]) for i in (1, 2, 4, 5)) < 1e-12
     assert all(abs(a.iterations[i] - b.iterations[i]) <= 1 for i in range(5))
