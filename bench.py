@@ -413,9 +413,11 @@ def run_mixed(args):
            "lognormal": bool(args.lognormal), "tol": 1e-10}
     ncell = cells * cells
     out["mixed_inner_solver"] = args.mixed_solver
-    for name, extra, mode in (("fp64", "tl_exit_true_residual", lib.DRIVER_RESIDENT),
-                              ("mixed", "tl_mixed_precision\ntl_mixed_inner_eps 1e-5",
-                               lib.DRIVER_PER_CALL)):
+    out["fp64_arithmetic"] = ARITHMETIC
+    for name, extra, mode in (("fp64", "tl_exit_true_residual\ntl_arithmetic %s" % ARITHMETIC,
+                               lib.DRIVER_RESIDENT),
+                              ("mixed", "tl_mixed_precision\ntl_mixed_inner_eps 1e-5\n"
+                               "tl_arithmetic %s" % ARITHMETIC, lib.DRIVER_PER_CALL)):
         solver = args.mixed_solver if name == "mixed" else "cg"
         deck = decks.five_state_deck(cells, solver=solver, prec="jac_diag",
                                      steps=args.steps, eps=1e-10, max_iters=100000,
@@ -460,7 +462,7 @@ def run_batch(args):
     import numpy as np
     from tealeaf_opencl_gb300 import decks, lib
     L = lib.load()
-    L.tea_gb300_set_arithmetic(1)
+    L.tea_gb300_set_arithmetic(lib.arithmetic_form(ARITHMETIC))
     problems = decks.batch_problems(args.problems, seed=args.seed)
     t0 = time.perf_counter()
     fields = [decks.paint(p) for p in problems]
@@ -503,7 +505,7 @@ def run_batch(args):
         seq_s, seq_ci = 0.0, 0.0
         for p in problems[:k]:
             deck = decks.batch_deck(p, steps=args.steps, eps=1e-12, prec="jac_diag",
-                                    arithmetic="fused")
+                                    arithmetic=ARITHMETIC)
             drv = lib.Driver(deck, mode=lib.DRIVER_RESIDENT)
             L.tea_gb300_synchronize()
             t0 = time.perf_counter()
@@ -559,7 +561,7 @@ def run_adjoint(args):
     en = lib.read_field("energy1")
     drv.close()
     L.tea_gb300_finalise()
-    L.tea_gb300_set_arithmetic(1)
+    L.tea_gb300_set_arithmetic(lib.arithmetic_form(ARITHMETIC))
     dev = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
     adj = lib.Adjoint(n, n)
     d, e = dev(dens), dev(en)
@@ -602,7 +604,7 @@ def run_adjoint(args):
     dens_s, en_s = lib.read_field("density"), lib.read_field("energy1")
     drv.close()
     L.tea_gb300_finalise()
-    L.tea_gb300_set_arithmetic(1)
+    L.tea_gb300_set_arithmetic(lib.arithmetic_form(ARITHMETIC))
     adj = lib.Adjoint(m, m)
     cfg_s = adj.config(steps, dt, 1e-15, 20000, 4)
     uo = torch.empty((m, m), dtype=torch.float64, device="cuda")
