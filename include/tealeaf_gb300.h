@@ -207,6 +207,13 @@ int tea_gb300_configure(int halo_depth, int solver, int preconditioner,
  * before tea_leaf_common_init_kernel_ocl_.  Returns 0, or -1 for another
  * value. */
 int tea_gb300_set_arithmetic(int form);
+/* How the driver's device-resident CG loop runs (TEA_DRIVER_RESIDENT):
+ * 0 (default) and 1 replay batches of iterations, three kernels each, from a
+ * CUDA graph; 2 runs the whole loop as one cooperative (persistent) launch
+ * with grid barriers between its phases.  The results are identical; on
+ * GB300 the persistent launch measured no faster at 512^2 to 4096^2.
+ * Returns 0, or -1 for another value. */
+int tea_gb300_set_resident_mode(int mode);
 int tea_gb300_get_arithmetic(void);
 
 /* 1 (default): fatal errors abort; 0: record and return. */

@@ -249,6 +249,7 @@ struct Config {
   bool set = false;
   int halo = 1, solver = SOLVER_JACOBI, prec = PREC_NONE, profiler = 0;
   int arith = 1;  // arithmetic form
+  int resident_mode = 0;
 };
 static Config g_config;
 
@@ -323,6 +324,7 @@ static bool init_chunk(int x_max, int y_max, const Config& cfg) {
   c.prec = cfg.prec;
   c.profiler_on = cfg.profiler != 0;
   c.arith = cfg.arith;
+  c.resident_mode = cfg.resident_mode;
   c.TH = reduction_rows(x_max, y_max);
   c.S = ((long long)(x_max + 2 * c.H + 1 + 31) / 32) * 32;
   c.rows = y_max + 2 * c.H + 1;
@@ -746,6 +748,17 @@ extern "C" int tea_gb300_set_arithmetic(int form) {
 }
 
 extern "C" int tea_gb300_get_arithmetic(void) { return chunk().arith; }
+
+extern "C" int tea_gb300_set_resident_mode(int mode) {
+  if (mode < 0 || mode > 2) {
+    fail(3, "tea_gb300_set_resident_mode: mode %d is not 0 (auto), 1 (graph) or 2 "
+            "(persistent)", mode);
+    return -1;
+  }
+  g_config.resident_mode = mode;
+  chunk().resident_mode = mode;
+  return 0;
+}
 
 extern "C" int tea_gb300_last_error(char* msg, int len) {
   const int code = g_err_code;

@@ -15,7 +15,7 @@ namespace tea {
 // the order of the per-lane sums are those of the row-by-row form.
 
 // w = A p and the lane's share of p.w (tea_leaf_cg_cl.cl:45-69)
-template <int TH, int F>
+template <int TH, int F, bool CG = false>
 __device__ __forceinline__ void cg_w_tile(const Dev& d, int x, int y0, bool xin,
                                           double* acc) {
 #pragma unroll 1
@@ -27,8 +27,8 @@ __device__ __forceinline__ void cg_w_tile(const Dev& d, int x, int y0, bool xin,
       pv[j] = 0.0;
       wv[j] = 0.0;
       if (xin && g + j < d.y_max) {
-        wv[j] = smvp<F>(d, d.p, c0 + j * d.S);
-        pv[j] = d.p[c0 + j * d.S];
+        wv[j] = smvp<F, CG>(d, d.p, c0 + j * d.S);
+        pv[j] = ldv<CG>(d.p + c0 + j * d.S);
       }
     }
 #pragma unroll
@@ -54,7 +54,7 @@ __device__ __forceinline__ void ur_values(double alpha, double& u, double p,
 
 // u += alpha p, r -= alpha w, z = M^-1 r and the lane's share of r.z (and
 // of r.r when NV == 2), tea_leaf_cg_cl.cl:73-137
-template <int TH, int F, int NV>
+template <int TH, int F, int NV, bool CG = false>
 __device__ __forceinline__ void cg_ur_tile(const Dev& d, int x, int y0, bool xin,
                                            double* acc, double alpha) {
 #pragma unroll 1
@@ -68,10 +68,10 @@ __device__ __forceinline__ void cg_ur_tile(const Dev& d, int x, int y0, bool xin
       uv[j] = pv[j] = rv[j] = wv[j] = mv[j] = 0.0;
       if (in[j]) {
         const long long c = c0 + j * d.S;
-        uv[j] = d.u[c];
-        pv[j] = d.p[c];
-        rv[j] = d.r[c];
-        wv[j] = d.w[c];
+        uv[j] = ldv<CG>(d.u + c);
+        pv[j] = ldv<CG>(d.p + c);
+        rv[j] = ldv<CG>(d.r + c);
+        wv[j] = ldv<CG>(d.w + c);
         if (d.prec == PREC_JAC_DIAG) mv[j] = d.Mi[c];
       }
     }
@@ -108,7 +108,7 @@ __device__ __forceinline__ void cg_ur_tile(const Dev& d, int x, int y0, bool xin
 
 // p = z + beta p, or r + beta p without a preconditioner
 // (tea_leaf_cg_cl.cl:141-160)
-template <int TH, int F>
+template <int TH, int F, bool CG = false>
 __device__ __forceinline__ void cg_p_tile(const Dev& d, int x, int y0, bool xin,
                                           double beta) {
   if (!xin) return;
@@ -121,8 +121,8 @@ __device__ __forceinline__ void cg_p_tile(const Dev& d, int x, int y0, bool xin,
     for (int j = 0; j < 4; j++) {
       sv[j] = pv[j] = 0.0;
       if (g + j < d.y_max) {
-        sv[j] = src[c0 + j * d.S];
-        pv[j] = d.p[c0 + j * d.S];
+        sv[j] = ldv<CG>(src + c0 + j * d.S);
+        pv[j] = ldv<CG>(d.p + c0 + j * d.S);
       }
     }
 #pragma unroll

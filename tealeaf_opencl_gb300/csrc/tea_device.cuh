@@ -61,7 +61,15 @@ __device__ __forceinline__ double bfly(double v) {
 // (e.g. tea_leaf_cg_cl.cl:59-63):
 //   (1 + (Ky_n + Ky_c) + (Kx_e + Kx_c)) x_c - (Ky_n x_n + Ky_c x_s)
 //                                           - (Kx_e x_e + Kx_c x_w)
-template <int F>
+// Load of a field value: plain, or with CG = true through L2 only
+// (ld.global.cg), for fields that other blocks of a persistent kernel write
+// while it runs (L1 is not coherent across SMs).
+template <bool CG>
+__device__ __forceinline__ double ldv(const double* p) {
+  return CG ? __ldcg(p) : *p;
+}
+
+template <int F, bool CG = false>
 __device__ __forceinline__ double smvp(const Dev& d, const double* x,
                                        long long c) {
   const long long S = d.S;
@@ -69,18 +77,18 @@ __device__ __forceinline__ double smvp(const Dev& d, const double* x,
   const double kxe = __ldg(d.Kx + c + 1), kxc = __ldg(d.Kx + c);
   const double D = __ldg(d.diag + c);
   if (!F)
-    return D * x[c] - (kyn * x[c + S] + kyc * x[c - S]) -
-           (kxe * x[c + 1] + kxc * x[c - 1]);
+    return D * ldv<CG>(x + c) - (kyn * ldv<CG>(x + c + S) + kyc * ldv<CG>(x + c - S)) -
+           (kxe * ldv<CG>(x + c + 1) + kxc * ldv<CG>(x + c - 1));
   if (F == 2) {
-    double t = D * x[c];
-    t = __fma_rn(-kyn, x[c + S], t);
-    t = __fma_rn(-kyc, x[c - S], t);
-    t = __fma_rn(-kxe, x[c + 1], t);
-    return __fma_rn(-kxc, x[c - 1], t);
+    double t = D * ldv<CG>(x + c);
+    t = __fma_rn(-kyn, ldv<CG>(x + c + S), t);
+    t = __fma_rn(-kyc, ldv<CG>(x + c - S), t);
+    t = __fma_rn(-kxe, ldv<CG>(x + c + 1), t);
+    return __fma_rn(-kxc, ldv<CG>(x + c - 1), t);
   }
-  const double t1 = __fma_rn(kyc, x[c - S], kyn * x[c + S]);
-  const double t2 = __fma_rn(kxc, x[c - 1], kxe * x[c + 1]);
-  return __fma_rn(D, x[c], -t1) - t2;
+  const double t1 = __fma_rn(kyc, ldv<CG>(x + c - S), kyn * ldv<CG>(x + c + S));
+  const double t2 = __fma_rn(kxc, ldv<CG>(x + c - 1), kxe * ldv<CG>(x + c + 1));
+  return __fma_rn(D, ldv<CG>(x + c), -t1) - t2;
 }
 
 // b - A x at offset c: the reference's "b - smvp" (calc_residual,
@@ -214,6 +222,64 @@ __device__ __forceinline__ void block_final_sum(const double* partials,
     }
     __syncthreads();
   }
+}
+
+// The same sum as block_final_sum for one value, handed to every thread of
+// the block instead of stored (used by persistent kernels, in which every
+// block forms the reduced value itself).  sh holds at least 9 doubles.
+__device__ __forceinline__ double block_final_value(const double* partials, int ns,
+                                                    double* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double a = 0.0;
+  for (int k = threadIdx.x; k < ns; k += kBlock) a = a + __ldcg(partials + k);
+  a = bfly(a);
+  if (lane == 0) sh[warp] = a;
+  __syncthreads();
+  if (warp == 0) {
+    double t = lane < 8 ? sh[lane] : 0.0;
+    t = bfly(t);
+    if (lane == 0) sh[8] = t;
+  }
+  __syncthreads();
+  const double v = sh[8];
+  __syncthreads();
+  return v;
+}
+
+// Barrier across every block of a cooperative launch (all blocks resident).
+// bar[0] counts arrivals, bar[1] is the generation.  Every thread's earlier
+// global writes are visible to every block after it.  A block waits at most
+// kBarrierSpins polls (about 4 s); on time-out, or when another block has
+// timed out, it sets *err and returns false, and the kernel must return.
+constexpr long long kBarrierSpins = 1LL << 26;
+__device__ __forceinline__ bool grid_barrier(unsigned int* bar, int* err) {
+  __shared__ int ok;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned int* gen = bar + 1;
+    const unsigned int g = *gen;
+    __threadfence();
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      long long spins = 0;
+      while (*gen == g) {
+        if (++spins > kBarrierSpins || *(volatile int*)err) {
+          atomicExch(err, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
 }
 
 // Last-block-done finish of the reduction; returns true in the block that

@@ -112,6 +112,8 @@ struct Chunk {
   double* res_coef = nullptr;          // device alphas/betas
   int res_coef_n = 0;
   unsigned int* res_counter = nullptr;
+  unsigned int* res_bar = nullptr;     // grid barrier [2] + error flag
+  int resident_mode = 0;               // 0 auto, 1 graph replay, 2 persistent
   cudaGraphExec_t res_graph = nullptr;
   int res_graph_iters = 0;
   bool res_graph_true_exit = false;

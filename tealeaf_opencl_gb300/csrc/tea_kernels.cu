@@ -1016,6 +1016,90 @@ static int tile_grid(Chunk& c, void (*kernel)(KArgs...)) {
   return (int)std::max<long long>(1, std::min<long long>(c.dev().ns, cap));
 }
 
+// The whole remaining CG loop as one cooperative launch, for grids whose
+// iterations are short enough for kernel boundaries to dominate.  Every
+// block keeps the same supertiles in all three phases; grid barriers
+// separate w = A p, the u/r/z update and p = z + beta p.  After each
+// reducing phase every block forms the reduced value itself from the
+// supertile partials, in the fixed order of block_final_sum, so all blocks
+// agree bit for bit and no extra barrier is needed; block 0 keeps the loop
+// state (cg_scalar_step).  Fields written by other blocks are read through
+// L2 (CG = true).  Results are those of the three-kernel loop.
+template <int TH, int F>
+__global__ void __launch_bounds__(kBlock)
+    k_cg_persistent(Dev d, Red red, ResState* st, unsigned int* bar, int* err) {
+  __shared__ double sh[16];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  Red rw = red, ru = red;
+  ru.partials = red.partials + red.stride;  // p.w and r.z partials apart
+  auto phase = [&](const Red& r, auto body, bool reduce) {
+    for (int s = blockIdx.x; s < d.ns; s += gridDim.x) {
+      const int sy = s / d.nsx, sx = s - sy * d.nsx;
+      const int tx = sx * kTilesPerSuper + warp;
+      double acc[1] = {0.0};
+      if (tx < d.ntx) {
+        const int x = tx * kTileW + lane;
+        body(x, sy * TH, x < d.x_max, acc);
+        if (reduce) acc[0] = bfly(acc[0]);
+      }
+      if (reduce) supertile_partial<1>(r, s, acc, sh);
+    }
+  };
+  for (;;) {
+    if (*(volatile int*)&st->stop) return;
+    const double rro = *(volatile double*)&st->rro;
+    phase(rw, [&](int x, int y0, bool xin, double* acc) {
+      cg_w_tile<TH, F, true>(d, x, y0, xin, acc);
+    }, true);
+    if (!grid_barrier(bar, err)) return;
+    const double pw = block_final_value(rw.partials, d.ns, sh);
+    const double alpha = rro / pw;
+    phase(ru, [&](int x, int y0, bool xin, double* acc) {
+      cg_ur_tile<TH, F, 1, true>(d, x, y0, xin, acc, alpha);
+    }, true);
+    if (!grid_barrier(bar, err)) return;
+    const double rrn = block_final_value(ru.partials, d.ns, sh);
+    const double beta = rrn / rro;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      st->pw = pw;
+      cg_scalar_step<1>(st, alpha, &rrn);
+      st->p_pending = 0;
+    }
+    phase(rw, [&](int x, int y0, bool xin, double* acc) {
+      cg_p_tile<TH, F, true>(d, x, y0, xin, beta);
+    }, false);
+    if (!grid_barrier(bar, err)) return;
+  }
+}
+
+// Cooperative launch of k_cg_persistent: as many blocks as can be resident
+// at once, at most one per supertile.  Returns false if the launch fails.
+template <int TH, int F>
+static bool launch_cg_persistent_t(Chunk& c) {
+  const void* fn = (const void*)k_cg_persistent<TH, F>;
+  const long long cap = (long long)c.num_sms * blocks_per_sm(fn);
+  const int grid = (int)std::max<long long>(1, std::min<long long>(c.dev().ns, cap));
+  Dev d = c.dev();
+  Red red = c.red();
+  ResState* st = c.res_state;
+  unsigned int* bar = c.res_bar;
+  int* err = (int*)(c.res_bar + 2);
+  void* args[] = {&d, &red, &st, &bar, &err};
+  return check_cuda(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kBlock), args, 0,
+                                                c.stream),
+                    "persistent CG launch");
+}
+
+static bool launch_cg_persistent(Chunk& c) {
+  if (c.TH == 16)
+    return c.arith == 2 ? launch_cg_persistent_t<16, 2>(c)
+           : c.arith == 1 ? launch_cg_persistent_t<16, 1>(c)
+                          : launch_cg_persistent_t<16, 0>(c);
+  return c.arith == 2 ? launch_cg_persistent_t<4, 2>(c)
+         : c.arith == 1 ? launch_cg_persistent_t<4, 1>(c)
+                        : launch_cg_persistent_t<4, 0>(c);
+}
+
 template <int TH, int F, int NV>
 static void enqueue_resident_iterations_t(Chunk& c, int iters) {
   const Dev d = c.dev();
@@ -1064,6 +1148,8 @@ void resident_release() {
   cudaFree(c.res_state);
   cudaFree(c.res_coef);
   cudaFree(c.res_counter);
+  cudaFree(c.res_bar);
+  c.res_bar = nullptr;
   cudaFreeHost(c.res_state_h);
   c.res_state = nullptr;
   c.res_coef = nullptr;
@@ -1078,6 +1164,18 @@ void resident_release() {
 // Kernels queued after the loop has stopped return at once.  The arithmetic
 // and the exit test are those of the per-call path, so the results are
 // bit-identical to it.
+// The persistent loop runs when asked for (resident_mode 2).  The default
+// is the graph loop: measured per CG iteration (jac_diag, chain form), the
+// graph loop took 24.3 / 51.7 / 150 / 455 us at 512^2 / 1024^2 / 2048^2 /
+// 4096^2 and the persistent one 25.3 / 56.3 / 154 / 455 us.  At small grids
+// every phase is latency-bound either way, and three grid barriers cost
+// what three graph-replayed launches cost; removing the barrier's back-off
+// or using one block per SM changed nothing.  The persistent loop keeps the
+// r.z exit test only (the true-residual exit uses the graph loop).
+static bool use_persistent(const Chunk& c, bool true_exit) {
+  return !true_exit && !c.profiler_on && c.resident_mode == 2;
+}
+
 int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
                            double eps_target, double* rro_out,
                            double* error_out, int* n_done, int* converged,
@@ -1101,7 +1199,9 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
         !check_cuda(cudaMallocHost(&c.res_state_h, sizeof(ResState)),
                     "cudaMallocHost state") ||
         !check_cuda(cudaMalloc(&c.res_counter, sizeof(unsigned int)),
-                    "cudaMalloc counter"))
+                    "cudaMalloc counter") ||
+        !check_cuda(cudaMalloc(&c.res_bar, 3 * sizeof(unsigned int)),
+                    "cudaMalloc barrier"))
       return -1;
     cudaMemsetAsync(c.res_counter, 0, sizeof(unsigned int), c.stream);
   }
@@ -1117,6 +1217,31 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
                                   cudaMemcpyHostToDevice, c.stream),
                   "resident state upload"))
     return -1;
+  if (use_persistent(c, true_exit)) {
+    // one cooperative launch runs the loop to its end
+    if (!check_cuda(cudaMemsetAsync(c.res_bar, 0, 3 * sizeof(unsigned int), c.stream),
+                    "barrier reset") ||
+        !launch_cg_persistent(c))
+      return -1;
+    count_launch("resident_cg_persistent");
+    int err = 0;
+    if (!check_cuda(cudaMemcpyAsync(&h, c.res_state, sizeof(ResState),
+                                    cudaMemcpyDeviceToHost, c.stream),
+                    "resident state read") ||
+        !check_cuda(cudaMemcpyAsync(&err, c.res_bar + 2, sizeof(int),
+                                    cudaMemcpyDeviceToHost, c.stream),
+                    "barrier flag read") ||
+        !check_cuda(cudaStreamSynchronize(c.stream), "persistent CG"))
+      return -1;
+    if (err) {
+      fail(25, "persistent CG: a grid barrier timed out");
+      return -1;
+    }
+    if (!h.stop) {
+      fail(24, "persistent CG loop ended before its exit test");
+      return -1;
+    }
+  } else {
   if (!c.res_graph && !c.profiler_on) {
     cudaGraph_t graph = nullptr;
     if (!check_cuda(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal),
@@ -1152,6 +1277,7 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
         !check_cuda(cudaStreamSynchronize(c.stream), "resident sync"))
       return -1;
     if (h.stop && !h.p_pending) break;
+  }
   }
   *rro_out = h.rro;
   *error_out = h.error;

@@ -5,8 +5,8 @@ tests/test_gpu_runs.py compares the GPU runs of test problems 2 and 3
 bit for bit: per-step iteration counts and the final temperature (as a hex
 float).  The oracle takes minutes to hours on a CPU for these, so the
 results are kept as a fixture: oracle_pins.json for the exact arithmetic
-form, oracle_pins_fused.json for the fused one.
-Usage: make_oracle_pins.py [--fused] TP [TP ...]
+form, oracle_pins_fused.json and oracle_pins_chain.json for the others.
+Usage: make_oracle_pins.py [--fused | --chain] TP [TP ...]
 """
 import json
 import os
@@ -19,20 +19,20 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from oracle import oracle  # noqa: E402
 
 
-def main(tps, fused):
-    path = os.path.join(HERE, "oracle_pins_fused.json" if fused else "oracle_pins.json")
+def main(tps, form):
+    path = os.path.join(HERE, "oracle_pins.json" if form == "exact"
+                        else "oracle_pins_%s.json" % form)
     pins = json.load(open(path)) if os.path.exists(path) else {}
     meta = json.load(open(os.path.join(HERE, "test_problems.json")))
     for tp in tps:
         p = meta["problems"][str(tp)]
         deck = open(os.path.join(HERE, p["deck"])).read()
-        deck = deck.replace("*endtea", "tl_arithmetic %s\n*endtea"
-                            % ("fused" if fused else "exact"), 1)
+        deck = deck.replace("*endtea", "tl_arithmetic %s\n*endtea" % form, 1)
         t0 = time.time()
         res = oracle.run_deck(deck)
         pins[str(tp)] = {
             "deck": p["deck"],
-            "arithmetic": "fused" if fused else "exact",
+            "arithmetic": form,
             "temp": res.final_temp,
             "temp_hex": float(res.final_temp).hex(),
             "golden_temp": p["temp"],
@@ -47,5 +47,5 @@ def main(tps, fused):
 
 if __name__ == "__main__":
     args = sys.argv[1:]
-    fused = "--fused" in args
-    main([int(a) for a in args if a != "--fused"] or [2], fused)
+    form = "fused" if "--fused" in args else "chain" if "--chain" in args else "exact"
+    main([int(a) for a in args if not a.startswith("--")] or [2], form)

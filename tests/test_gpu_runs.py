@@ -25,7 +25,7 @@ def problem(tp):
 
 
 def pins(mode):
-    name = "oracle_pins_fused.json" if mode == "fused" else "oracle_pins.json"
+    name = "oracle_pins.json" if mode == "exact" else "oracle_pins_%s.json" % mode
     path = os.path.join(GOLD, name)
     return json.load(open(path)) if os.path.exists(path) else {}
 
@@ -60,7 +60,7 @@ def test_test_problem_matches_golden_and_oracle(tp, mode):
     assert_matches_oracle(steps, oracle.run_deck(deck))
 
 
-@pytest.mark.parametrize("mode", ["exact", "fused"])
+@pytest.mark.parametrize("mode", ["exact", "fused", "chain"])
 @pytest.mark.parametrize("tp", [2, 3])
 def test_cg_test_problem_matches_golden_and_oracle_pin(tp, mode):
     deck, temp = problem(tp)
@@ -112,3 +112,29 @@ def test_reflective_check_result_deck_matches_oracle():
     res = oracle.run_deck(deck)
     assert_matches_oracle(steps, res)
     assert [s.exact_error for s in steps] == list(res.exact_error[:res.n_steps])
+
+
+@pytest.mark.parametrize("cells,y_cells,prec,mode", [(512, 512, "jac_diag", "chain"),
+                                                    (300, 211, "jac_block", "fused"),
+                                                    (2048, 2440, "none", "exact")])
+def test_persistent_and_graph_resident_loops_agree(cells, y_cells, prec, mode):
+    """The resident CG loop as one cooperative launch (grid barriers between
+    its phases) gives the same iteration counts and field summaries, bit for
+    bit, as the graph-replayed three-kernel loop; small decks also against
+    the oracle."""
+    L = lib.load()
+    deck = decks.five_state_deck(cells, solver="cg", prec=prec, steps=3, eps=1e-15,
+                                 max_iters=5000, y_cells=y_cells,
+                                 extra="tl_arithmetic %s" % mode)
+    try:
+        L.tea_gb300_set_resident_mode(1)
+        graph = gpu_run(deck, mode=lib.DRIVER_RESIDENT)
+        L.tea_gb300_set_resident_mode(2)
+        persistent = gpu_run(deck, mode=lib.DRIVER_RESIDENT)
+    finally:
+        L.tea_gb300_set_resident_mode(0)
+    assert [s.iterations for s in graph] == [s.iterations for s in persistent]
+    a, b = graph[-1], persistent[-1]
+    assert (a.vol, a.mass, a.ie, a.temp) == (b.vol, b.mass, b.ie, b.temp)
+    if cells * y_cells <= 512 * 512:
+        assert_matches_oracle(persistent, oracle.run_deck(deck))
