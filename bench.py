@@ -224,7 +224,6 @@ def run_ours(args, dist):
     drv = lib.Driver(deck, mode=lib.DRIVER_RESIDENT, max_iters_cap=args.cap)
     for _ in range(args.warmup):
         drv.step()
-    L.tea_gb300_kernel_timer_select(kernel.encode())
     clocks = Clocks(0)
     dist.barrier()
     L.tea_gb300_synchronize()
@@ -240,9 +239,6 @@ def run_ours(args, dist):
     dist.barrier()
     ms = float(L.tea_gb300_event_elapsed_ms(0, 1))
     launches = L.tea_gb300_kernel_launches() - launches0
-    kms, kn = ctypes.c_double(), ctypes.c_longlong()
-    L.tea_gb300_kernel_timer_read(ctypes.byref(kms), ctypes.byref(kn))
-    L.tea_gb300_kernel_timer_select(b"")
     drv.close()
     outer = sum(i.iterations for i in infos)
     inner = sum(i.inner_iterations for i in infos)
@@ -262,6 +258,10 @@ def run_ours(args, dist):
     chunk_write = lambda f, a: L.tea_gb300_write_field(lib.FIELD[f], a.ctypes.data_as(lib.PD))
     chunk_read("density", host[0])
     chunk_read("energy1", host[1])
+    # the dominant kernel's launches are timed with CUDA events during this
+    # pass: the per-call path launches it on its own (the resident loop
+    # replays it inside graphs)
+    L.tea_gb300_kernel_timer_select(kernel.encode())
     dist.barrier()
     L.tea_gb300_synchronize()
     t0 = time.perf_counter()
@@ -275,6 +275,9 @@ def run_ours(args, dist):
         e2e_outer += info.iterations + info.inner_iterations
     L.tea_gb300_synchronize()
     e2e_s = time.perf_counter() - t0
+    kms, kn = ctypes.c_double(), ctypes.c_longlong()
+    L.tea_gb300_kernel_timer_read(ctypes.byref(kms), ctypes.byref(kn))
+    L.tea_gb300_kernel_timer_select(b"")
     dist.barrier()
     drv.close()
     for b in bufs:

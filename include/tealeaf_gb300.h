@@ -333,7 +333,7 @@ void tea_gb300_host_free(void* p);
 
 /* Solve-loop implementations the driver can use. */
 #define TEA_DRIVER_PER_CALL 0  /* reference call sequence, host scalars */
-#define TEA_DRIVER_RESIDENT 1  /* CG iterations kept on the device */
+#define TEA_DRIVER_RESIDENT 1  /* CG and PPCG iterations kept on the device */
 
 typedef struct {
   int step;               /* timestep number */

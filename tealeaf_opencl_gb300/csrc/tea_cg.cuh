@@ -53,10 +53,14 @@ __device__ __forceinline__ void ur_values(double alpha, double& u, double p,
 }
 
 // u += alpha p, r -= alpha w, z = M^-1 r and the lane's share of r.z (and
-// of r.r when NV == 2), tea_leaf_cg_cl.cl:73-137
-template <int TH, int F, int NV, bool CG = false>
+// of r.r when NV == 2; no sum when NV == 0), tea_leaf_cg_cl.cl:73-137.
+// With SD it also starts PPCG's inner steps, sd = M^-1 r / theta
+// (tea_leaf_ppcg_cl.cl:4-60), from the z it has just formed: the same
+// values tea_leaf_ppcg_solve_init_sd computes from the stored r.
+template <int TH, int F, int NV, bool CG = false, bool SD = false>
 __device__ __forceinline__ void cg_ur_tile(const Dev& d, int x, int y0, bool xin,
-                                           double* acc, double alpha) {
+                                           double* acc, double alpha,
+                                           double theta = 1.0) {
 #pragma unroll 1
   for (int g = y0; g < y0 + TH; g += 4) {
     const long long c0 = cidx(d, x, g);
@@ -97,10 +101,11 @@ __device__ __forceinline__ void cg_ur_tile(const Dev& d, int x, int y0, bool xin
       double av = 0.0, bv = 0.0;
       if (in[j]) {
         if (d.prec != PREC_NONE) d.z[c0 + j * d.S] = zv[j];
+        if (SD) d.sd[c0 + j * d.S] = (d.prec != PREC_NONE ? zv[j] : rv[j]) / theta;
         av = rv[j];
         bv = d.prec != PREC_NONE ? zv[j] : rv[j];
       }
-      acc[0] = accum<F>(acc[0], av, bv);
+      if (NV > 0) acc[0] = accum<F>(acc[0], av, bv);
       if (NV > 1) acc[NV - 1] = accum<F>(acc[NV - 1], av, av);
     }
   }

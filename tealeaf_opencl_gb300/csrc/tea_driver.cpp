@@ -591,6 +591,24 @@ class Driver {
           if (cheby_calc_steps == 0)
             tea_leaf_ppcg_init_ocl_(ch_alphas.data(), ch_betas.data(), &theta,
                                     &D.inner_steps);
+          if (mode == TEA_DRIVER_RESIDENT) {
+            // the remaining PPCG iterations on the device; they stop
+            // exactly where this loop would
+            int n_done = 0, conv = 0;
+            if (tea::resident_ppcg_iterations(n, loop_max, rro, D.eps * initial_residual,
+                                              &rro, &error, &n_done, &conv) != 0)
+              return -1;
+            const int done = n_done - n + 1;
+            ppcg_inner_iters += D.inner_steps * done;
+            cheby_calc_steps += done;
+            n = n_done;
+            if (conv) {
+              exited = true;
+              break;
+            }
+            n++;
+            continue;
+          }
           tea_leaf_cg_calc_w_kernel_ocl_(&pw);
           alpha = rro / pw;
           tea_leaf_cg_calc_ur_kernel_ocl_(&alpha, &rrn);

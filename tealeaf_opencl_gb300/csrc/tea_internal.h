@@ -113,6 +113,8 @@ struct Chunk {
   int res_coef_n = 0;
   unsigned int* res_counter = nullptr;
   unsigned int* res_bar = nullptr;     // grid barrier [2] + error flag
+  cudaGraphExec_t res_ppcg_graph = nullptr;  // resident PPCG iterations
+  std::vector<double> res_ppcg_key;          // theta, coefficients, form of it
   int resident_mode = 0;               // 0 auto, 1 graph replay, 2 persistent
   cudaGraphExec_t res_graph = nullptr;
   int res_graph_iters = 0;
@@ -205,6 +207,12 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
                            double* error_out, int* n_done, int* converged,
                            double* cg_alphas, double* cg_betas,
                            bool true_exit = false);
+// device-resident PPCG iterations n_begin..loop_max with the coefficients
+// of the last tea_leaf_ppcg_init_ocl_ (tea_solve.f90:231-268); the fused
+// calc_ur + init_sd kernel replaces the per-call pair
+int resident_ppcg_iterations(int n_begin, int loop_max, double rro_in,
+                             double eps_target, double* rro_out, double* error_out,
+                             int* n_done, int* converged);
 void resident_release();
 // mixed-precision solve (tea_mixed.cu)
 void mixed_release();

@@ -553,7 +553,8 @@ __global__ void __launch_bounds__(kBlock) k_cheby_calc_u(Dev d, Red red) {
 template <int TH, int F>
 __global__ void __launch_bounds__(kBlock)
     k_ppcg_sd(Dev d, Red red, int mode, double theta, double alpha,
-              double beta) {
+              double beta, const ResState* st) {
+  if (st && *(volatile const int*)&st->stop) return;
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
     if (d.prec == PREC_JAC_BLOCK) {
@@ -613,7 +614,9 @@ __global__ void __launch_bounds__(kBlock)
 
 // tea_leaf_ppcg_solve_update_r, tea_leaf_ppcg_cl.cl:62-88
 template <int TH, int F>
-__global__ void __launch_bounds__(kBlock) k_ppcg_update_r(Dev d, Red red) {
+__global__ void __launch_bounds__(kBlock)
+    k_ppcg_update_r(Dev d, Red red, const ResState* st) {
+  if (st && *(volatile const int*)&st->stop) return;
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
 #pragma unroll 1
@@ -861,17 +864,17 @@ void launch_cheby_calc_u(Chunk& c) {
 
 void launch_ppcg_init_sd(Chunk& c, double theta) {
   TH_DISPATCH(c, "tea_leaf_ppcg_solve_init_sd", k_ppcg_sd, c.dev(), c.red(), 0,
-              theta, 0.0, 0.0);
+              theta, 0.0, 0.0, (const ResState*)nullptr);
 }
 
 void launch_ppcg_update_r(Chunk& c) {
   TH_DISPATCH(c, "tea_leaf_ppcg_solve_update_r", k_ppcg_update_r, c.dev(),
-              c.red());
+              c.red(), (const ResState*)nullptr);
 }
 
 void launch_ppcg_calc_sd(Chunk& c, double alpha, double beta) {
   TH_DISPATCH(c, "tea_leaf_ppcg_solve_calc_sd", k_ppcg_sd, c.dev(), c.red(), 1,
-              0.0, alpha, beta);
+              0.0, alpha, beta, (const ResState*)nullptr);
 }
 
 void launch_jacobi_copy_u(Chunk& c) {
@@ -1100,6 +1103,85 @@ static bool launch_cg_persistent(Chunk& c) {
                         : launch_cg_persistent_t<4, 0>(c);
 }
 
+// ---- device-resident PPCG iterations (tea_solve.f90:231-268 after the
+// switch from CG), scalars in the ResState as for CG ----
+
+// tea_leaf_cg_calc_ur of a PPCG iteration with alpha = rro/pw from the loop
+// state, fused with tea_leaf_ppcg_init_sd: PPCG discards this r.z, so no
+// sum is taken, and sd = M^-1 r / theta comes from the z formed here.
+template <int TH, int F>
+__global__ void __launch_bounds__(kBlock)
+    k_ppcg_ur_sd(Dev d, Red red, ResState* st, double theta) {
+  if (*(volatile int*)&st->stop) return;
+  const double alpha = st->rro / st->pw;
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    cg_ur_tile<TH, F, 0, false, true>(d, x, y0, xin, acc, alpha, theta);
+  });
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->alpha = alpha;
+}
+
+// tea_leaf_ppcg_calc_zrnorm (r.z with the z of the last calc_ur) with the
+// host steps of the iteration: beta, rro = rrn, error, the exit test.
+template <int TH, int F>
+__global__ void __launch_bounds__(kBlock) k_ppcg_rz_step(Dev d, Red red, ResState* st) {
+  if (*(volatile int*)&st->stop) return;
+  const double* zz = d.prec != PREC_NONE ? d.z : d.r;
+  const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+#pragma unroll 4
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      double av = 0.0, bv = 0.0;
+      if (xin && y < d.y_max) {
+        const long long c = cidx(d, x, y);
+        av = d.r[c];
+        bv = zz[c];
+      }
+      acc[0] = accum<F>(acc[0], av, bv);
+    }
+  });
+  if (last && threadIdx.x == 0) {
+    cg_scalar_step<1>(st, st->alpha, red.result);
+    __threadfence();
+  }
+}
+
+template <int TH, int F>
+static void enqueue_ppcg_iterations_t(Chunk& c, int iters) {
+  const Dev d = c.dev();
+  const Red red = c.red();
+  ResState* st = c.res_state;
+  const double theta = c.ppcg_theta;
+  const int gw = tile_grid(c, k_cg_calc_w<TH, F>);
+  const int gu = tile_grid(c, k_ppcg_ur_sd<TH, F>);
+  const int gr = tile_grid(c, k_ppcg_update_r<TH, F>);
+  const int gs = tile_grid(c, k_ppcg_sd<TH, F>);
+  const int gz = tile_grid(c, k_ppcg_rz_step<TH, F>);
+  const int gp = tile_grid(c, k_cg_calc_p<TH, F>);
+  for (int i = 0; i < iters; i++) {
+    k_cg_calc_w<TH, F><<<gw, kBlock, 0, c.stream>>>(d, red, st);
+    k_ppcg_ur_sd<TH, F><<<gu, kBlock, 0, c.stream>>>(d, red, st, theta);
+    for (int k = 0; k < c.n_ppcg; k++) {
+      k_ppcg_update_r<TH, F><<<gr, kBlock, 0, c.stream>>>(d, red, st);
+      k_ppcg_sd<TH, F><<<gs, kBlock, 0, c.stream>>>(d, red, 1, 0.0, c.ppcg_alpha_h[k],
+                                                    c.ppcg_beta_h[k], st);
+    }
+    k_ppcg_rz_step<TH, F><<<gz, kBlock, 0, c.stream>>>(d, red, st);
+    k_cg_calc_p<TH, F><<<gp, kBlock, 0, c.stream>>>(d, red, 0.0, st, c.res_counter);
+  }
+}
+
+static void enqueue_ppcg_iterations(Chunk& c, int iters) {
+  if (c.TH == 16) {
+    if (c.arith == 2) enqueue_ppcg_iterations_t<16, 2>(c, iters);
+    else if (c.arith == 1) enqueue_ppcg_iterations_t<16, 1>(c, iters);
+    else enqueue_ppcg_iterations_t<16, 0>(c, iters);
+  } else {
+    if (c.arith == 2) enqueue_ppcg_iterations_t<4, 2>(c, iters);
+    else if (c.arith == 1) enqueue_ppcg_iterations_t<4, 1>(c, iters);
+    else enqueue_ppcg_iterations_t<4, 0>(c, iters);
+  }
+}
+
 template <int TH, int F, int NV>
 static void enqueue_resident_iterations_t(Chunk& c, int iters) {
   const Dev d = c.dev();
@@ -1150,6 +1232,9 @@ void resident_release() {
   cudaFree(c.res_counter);
   cudaFree(c.res_bar);
   c.res_bar = nullptr;
+  if (c.res_ppcg_graph) cudaGraphExecDestroy(c.res_ppcg_graph);
+  c.res_ppcg_graph = nullptr;
+  c.res_ppcg_key.clear();
   cudaFreeHost(c.res_state_h);
   c.res_state = nullptr;
   c.res_coef = nullptr;
@@ -1293,6 +1378,88 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
     if (!check_cuda(cudaStreamSynchronize(c.stream), "resident coefficients"))
       return -1;
   }
+  return 0;
+}
+
+// PPCG iterations n_begin..loop_max with all scalars on the device, batches
+// of 4 iterations replayed from a captured graph until the loop stops.  The
+// kernels and the exit test are those of the per-call path (whose
+// calc_ur + init_sd pair is fused here), so results are bit-identical.
+int resident_ppcg_iterations(int n_begin, int loop_max, double rro_in,
+                             double eps_target, double* rro_out, double* error_out,
+                             int* n_done, int* converged) {
+  Chunk& c = chunk();
+  if (c.n_ppcg < 1) {
+    fail(26, "resident PPCG: no coefficients (tea_leaf_ppcg_init_ocl_ first)");
+    return -1;
+  }
+  const int batch = 4;
+  if (!c.res_state) {
+    if (!check_cuda(cudaMalloc(&c.res_state, sizeof(ResState)), "cudaMalloc state") ||
+        !check_cuda(cudaMallocHost(&c.res_state_h, sizeof(ResState)),
+                    "cudaMallocHost state") ||
+        !check_cuda(cudaMalloc(&c.res_counter, sizeof(unsigned int)),
+                    "cudaMalloc counter") ||
+        !check_cuda(cudaMalloc(&c.res_bar, 3 * sizeof(unsigned int)),
+                    "cudaMalloc barrier"))
+      return -1;
+    cudaMemsetAsync(c.res_counter, 0, sizeof(unsigned int), c.stream);
+  }
+  std::vector<double> key = {c.ppcg_theta, (double)c.arith, (double)c.n_ppcg};
+  key.insert(key.end(), c.ppcg_alpha_h, c.ppcg_alpha_h + c.n_ppcg);
+  key.insert(key.end(), c.ppcg_beta_h, c.ppcg_beta_h + c.n_ppcg);
+  if (c.res_ppcg_graph && key != c.res_ppcg_key) {
+    cudaGraphExecDestroy(c.res_ppcg_graph);
+    c.res_ppcg_graph = nullptr;
+  }
+  ResState& h = *c.res_state_h;
+  memset(&h, 0, sizeof(h));
+  h.rro = rro_in;
+  h.eps_target = eps_target;
+  h.n = n_begin;
+  h.loop_max = loop_max;
+  if (!check_cuda(cudaMemcpyAsync(c.res_state, &h, sizeof(ResState),
+                                  cudaMemcpyHostToDevice, c.stream),
+                  "resident state upload"))
+    return -1;
+  if (!c.res_ppcg_graph && !c.profiler_on) {
+    cudaGraph_t graph = nullptr;
+    if (!check_cuda(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal),
+                    "graph capture"))
+      return -1;
+    enqueue_ppcg_iterations(c, batch);
+    if (!check_cuda(cudaStreamEndCapture(c.stream, &graph), "graph capture end") ||
+        !check_cuda(cudaGraphInstantiate(&c.res_ppcg_graph, graph, 0), "graph instantiate"))
+      return -1;
+    cudaGraphDestroy(graph);
+    c.res_ppcg_key = key;
+  }
+  const int per_iter = 4 + 2 * c.n_ppcg;
+  const long long max_batches = (long long)(loop_max - n_begin) / batch + 3;
+  for (long long nb = 0;; nb++) {
+    if (nb >= max_batches) {
+      fail(24, "resident PPCG loop did not stop after %lld batches", nb);
+      return -1;
+    }
+    if (c.res_ppcg_graph) {
+      if (!check_cuda(cudaGraphLaunch(c.res_ppcg_graph, c.stream), "graph launch"))
+        return -1;
+    } else {
+      enqueue_ppcg_iterations(c, batch);
+      check_cuda(cudaGetLastError(), "resident PPCG launch");
+    }
+    count_launches((long long)batch * per_iter);
+    if (!check_cuda(cudaMemcpyAsync(&h, c.res_state, sizeof(ResState),
+                                    cudaMemcpyDeviceToHost, c.stream),
+                    "resident state read") ||
+        !check_cuda(cudaStreamSynchronize(c.stream), "resident sync"))
+      return -1;
+    if (h.stop && !h.p_pending) break;
+  }
+  *rro_out = h.rro;
+  *error_out = h.error;
+  *n_done = h.n;
+  *converged = h.converged;
   return 0;
 }
 

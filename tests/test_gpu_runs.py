@@ -101,7 +101,27 @@ def test_cheby_ppcg_decks_match_oracle(solver, prec, mode):
     deck = decks.five_state_deck(256, solver=solver, prec=prec, steps=4, eps=1e-15,
                                  max_iters=5000, halo=2, inner_steps=10, presteps=20,
                                  extra="tl_arithmetic %s" % mode)
-    assert_matches_oracle(gpu_run(deck), oracle.run_deck(deck))
+    res = oracle.run_deck(deck)
+    assert_matches_oracle(gpu_run(deck), res)
+    if solver == "ppcg":
+        # the device-resident PPCG loop (fused calc_ur + init_sd, scalars on
+        # the device) stops at the same iteration with the same bits
+        assert_matches_oracle(gpu_run(deck, mode=lib.DRIVER_RESIDENT), res)
+
+
+@pytest.mark.parametrize("prec,eps,steps", [("jac_block", 1e-10, 3), ("jac_diag", 1e-15, 2),
+                                            ("none", 1e-8, 3)])
+def test_resident_ppcg_matches_per_call(prec, eps, steps):
+    """Converging and capped PPCG runs, tall tiles: resident = per-call."""
+    deck = decks.five_state_deck(2048, solver="ppcg", prec=prec, steps=steps, eps=eps,
+                                 max_iters=300, y_cells=2440, inner_steps=8, presteps=15,
+                                 summary_frequency=0, extra="tl_arithmetic chain")
+    a = gpu_run(deck)
+    b = gpu_run(deck, mode=lib.DRIVER_RESIDENT)
+    assert [s.iterations for s in a] == [s.iterations for s in b]
+    assert [s.inner_iterations for s in a] == [s.inner_iterations for s in b]
+    assert (a[-1].vol, a[-1].mass, a[-1].ie, a[-1].temp) == \
+        (b[-1].vol, b[-1].mass, b[-1].ie, b[-1].temp)
 
 
 def test_reflective_check_result_deck_matches_oracle():
