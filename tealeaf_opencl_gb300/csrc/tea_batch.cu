@@ -88,6 +88,42 @@ __device__ __forceinline__ void run_supertile(const Dev& d, int s, double* acc,
   }
 }
 
+// The supertile partial sums of supertiles s0..s1-1 of a problem (one
+// value), four supertiles at a time with the shared butterflies of
+// tea_device.cuh (bfly4, supertile_partials4): the same sums as one
+// run_supertile and supertile_partial per supertile.  sh holds 32 doubles.
+template <class Body>
+__device__ __forceinline__ void unit_partials(const Dev& d, const Red& red, int s0,
+                                              int s1, double* sh, Body body) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int g = s0; g < s1; g += 4) {
+    double tiles[4];
+    int s_k[4];
+#pragma unroll 1
+    for (int k = 0; k < 4; k++) {
+      double acc[1] = {0.0};
+      const int s = g + k;
+      if (s < s1) {
+        const int sy = s / d.nsx, sx = s - sy * d.nsx;
+        const int tx = sx * kTilesPerSuper + warp;
+        if (tx < d.ntx) {
+          const int x = tx * kTileW + lane;
+          body(x, sy * d.th, x < d.x_max, acc);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (q == k) {
+          tiles[q] = acc[0];
+          s_k[q] = s < s1 ? s : d.ns;
+        }
+    }
+    const double t = bfly4(tiles[0], tiles[1], tiles[2], tiles[3]);
+    if ((lane & 7) == 0) sh[bfly4_slot(lane) * 8 + warp] = t;
+    supertile_partials4<1>(red, s_k, d.ns, sh);
+  }
+}
+
 // Counts one finished unit of a problem; true in the block that finished
 // the problem's last one, which also resets the counter.
 __device__ __forceinline__ bool unit_done(unsigned int* counter, int units,
@@ -110,7 +146,7 @@ template <int F>
 __global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
     k_b_calc_w(const Dev* __restrict__ devs, const Red* __restrict__ reds,
                ResState* st, WorkList wl) {
-  __shared__ double sh[8];
+  __shared__ double sh[32];
   __shared__ unsigned int is_last;
   const int U = wl.counts[0], np = wl.counts[1];
   for (int u = blockIdx.x; u < U; u += gridDim.x) {
@@ -120,16 +156,12 @@ __global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
     const Dev d = devs[i];
     const Red red = reds[i];
     const int s0 = (u - wl.ustart[j]) * wl.G, s1 = min(s0 + wl.G, d.ns);
-    for (int s = s0; s < s1; s++) {
-      double acc[1];
-      run_supertile<1>(d, s, acc, [&](int x, int y0, bool xin, double* a) {
-        if (d.th == 16)
-          cg_w_tile<16, F>(d, x, y0, xin, a);
-        else
-          cg_w_tile<4, F>(d, x, y0, xin, a);
-      });
-      supertile_partial<1>(red, s, acc, sh);
-    }
+    unit_partials(d, red, s0, s1, sh, [&](int x, int y0, bool xin, double* a) {
+      if (d.th == 16)
+        cg_w_tile<16, F>(d, x, y0, xin, a);
+      else
+        cg_w_tile<4, F>(d, x, y0, xin, a);
+    });
     if (unit_done(red.counter, units_of(d.ns, wl.G), &is_last)) {
       block_final_sum<1>(red.partials, red.stride, d.ns, red.result, sh);
       if (threadIdx.x == 0) {
@@ -147,7 +179,7 @@ template <int F>
 __global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
     k_b_calc_ur(const Dev* __restrict__ devs, const Red* __restrict__ reds,
                 ResState* st, WorkList wl) {
-  __shared__ double sh[8];
+  __shared__ double sh[32];
   __shared__ unsigned int is_last;
   const int U = wl.counts[0], np = wl.counts[1];
   for (int u = blockIdx.x; u < U; u += gridDim.x) {
@@ -158,16 +190,12 @@ __global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
     const Red red = reds[i];
     const double alpha = st[i].rro / st[i].pw;
     const int s0 = (u - wl.ustart[j]) * wl.G, s1 = min(s0 + wl.G, d.ns);
-    for (int s = s0; s < s1; s++) {
-      double acc[1];
-      run_supertile<1>(d, s, acc, [&](int x, int y0, bool xin, double* a) {
-        if (d.th == 16)
-          cg_ur_tile<16, F, 1>(d, x, y0, xin, a, alpha);
-        else
-          cg_ur_tile<4, F, 1>(d, x, y0, xin, a, alpha);
-      });
-      supertile_partial<1>(red, s, acc, sh);
-    }
+    unit_partials(d, red, s0, s1, sh, [&](int x, int y0, bool xin, double* a) {
+      if (d.th == 16)
+        cg_ur_tile<16, F, 1>(d, x, y0, xin, a, alpha);
+      else
+        cg_ur_tile<4, F, 1>(d, x, y0, xin, a, alpha);
+    });
     if (unit_done(red.counter, units_of(d.ns, wl.G), &is_last)) {
       block_final_sum<1>(red.partials, red.stride, d.ns, red.result, sh);
       if (threadIdx.x == 0) {

@@ -302,33 +302,115 @@ __device__ __forceinline__ bool finish_reduction(const Red& red, int ns,
   return true;
 }
 
-// Walks the block's supertiles; body(x, y0, xin, acc) processes the TH rows
-// of one lane's column x starting at interior row y0 and adds its
-// contributions row by row into acc[0..NV).  Returns true in the one block
-// that finished the reduction (thread 0 of it holds red.result).
+// Four xor butterflies (bfly) at once.  a0..a3 are this lane's values of
+// four tiles.  Each stage adds exactly the pairs bfly adds, so every tile
+// sum is bit-identical to bfly's; but the tiles share the instructions: 6
+// FP64 additions for four tiles instead of 20.  On GB300 the FP64 pipe
+// charges a whole warp instruction however few lanes are active, so the
+// sharing is what saves time.  On return lanes 0-7 hold tile 0's sum,
+// 16-23 tile 1's, 8-15 tile 2's and 24-31 tile 3's.
+__device__ __forceinline__ double bfly4(double a0, double a1, double a2, double a3) {
+  const int lane = threadIdx.x & 31;
+  const bool hi16 = lane & 16, hi8 = lane & 8;
+  // off 16: lanes 0-15 carry tiles 0 and 2, lanes 16-31 tiles 1 and 3
+  const double r1 = (hi16 ? a1 : a0) +
+                    __shfl_xor_sync(0xffffffffu, hi16 ? a0 : a1, 16);
+  const double r2 = (hi16 ? a3 : a2) +
+                    __shfl_xor_sync(0xffffffffu, hi16 ? a2 : a3, 16);
+  // off 8: lanes with bit 8 clear keep r1's tile, lanes with it set r2's
+  double r = (hi8 ? r2 : r1) + __shfl_xor_sync(0xffffffffu, hi8 ? r1 : r2, 8);
+#pragma unroll
+  for (int off = 4; off >= 1; off >>= 1) r = r + __shfl_xor_sync(0xffffffffu, r, off);
+  return r;
+}
+
+// The slot (0-3) of the tile whose sum bfly4 leaves in this lane's group.
+__device__ __forceinline__ int bfly4_slot(int lane) {
+  return ((lane >> 4) & 1) | ((lane >> 2) & 2);
+}
+
+// Steps 3 of the summation order for four supertiles at once: sh[v*32 +
+// k*8 + w] holds warp w's tile sum of value v in supertile k; warp 0 forms
+// each supertile sum exactly as supertile_partial does (lanes 8-31 of that
+// butterfly hold +0.0, so its first two stages add +0.0 and the last three
+// add within lanes 0-7) and stores it at partials[v][s_k].  Called by the
+// whole block.
+template <int NV>
+__device__ __forceinline__ void supertile_partials4(const Red& red, const int* s_k,
+                                                    int ns, double* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      double t = sh[v * 32 + lane];
+      t = t + 0.0;  // the two +0.0 stages: (t + 0) + 0 == t + 0
+#pragma unroll
+      for (int off = 4; off >= 1; off >>= 1) t = t + __shfl_xor_sync(0xffffffffu, t, off);
+      const int k = lane >> 3;
+      if ((lane & 7) == 0 && s_k[k] < ns) red.partials[v * red.stride + s_k[k]] = t;
+    }
+  }
+  __syncthreads();
+}
+
+// Walks the block's supertiles (s = blockIdx.x + j*gridDim.x) four at a
+// time; body(x, y0, xin, acc) processes the TH rows of one lane's column x
+// starting at interior row y0 and adds its contributions row by row into
+// acc[0..NV).  Returns true in the one block that finished the reduction
+// (thread 0 of it holds red.result).
 template <int TH, int NV, class Body>
 __device__ __forceinline__ bool tile_driver(const Dev& d, const Red& red,
                                             Body body) {
-  __shared__ double sh[(NV > 0 ? NV : 1) * 8];
+  constexpr int NVV = NV > 0 ? NV : 1;
+  __shared__ double sh[NVV * 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int s = blockIdx.x; s < d.ns; s += gridDim.x) {
-    const int sy = s / d.nsx, sx = s - sy * d.nsx;
-    const int tx = sx * kTilesPerSuper + warp;
-    double acc[NV > 0 ? NV : 1];
-#pragma unroll
-    for (int v = 0; v < (NV > 0 ? NV : 1); v++) acc[v] = 0.0;
-    if (tx < d.ntx) {
-      const int x = tx * kTileW + lane;
-      body(x, sy * TH, x < d.x_max, acc);
-      if (NV > 0) {
-#pragma unroll
-        for (int v = 0; v < NV; v++) acc[v] = bfly(acc[v]);
+  if (NV == 0) {
+    for (int s = blockIdx.x; s < d.ns; s += gridDim.x) {
+      const int sy = s / d.nsx, sx = s - sy * d.nsx;
+      const int tx = sx * kTilesPerSuper + warp;
+      double acc[NVV] = {0.0};
+      if (tx < d.ntx) {
+        const int x = tx * kTileW + lane;
+        body(x, sy * TH, x < d.x_max, acc);
       }
     }
-    if (NV > 0) supertile_partial<NV>(red, s, acc, sh);
+    return false;
   }
-  if (NV > 0) return finish_reduction<NV>(red, d.ns, sh);
-  return false;
+  for (int s0 = blockIdx.x; s0 < d.ns; s0 += 4 * gridDim.x) {
+    double tiles[4][NVV];
+    int s_k[4];
+#pragma unroll 1
+    for (int k = 0; k < 4; k++) {
+      double acc[NVV];
+#pragma unroll
+      for (int v = 0; v < NVV; v++) acc[v] = 0.0;
+      const int s = s0 + k * gridDim.x;
+      if (s < d.ns) {
+        const int sy = s / d.nsx, sx = s - sy * d.nsx;
+        const int tx = sx * kTilesPerSuper + warp;
+        if (tx < d.ntx) {
+          const int x = tx * kTileW + lane;
+          body(x, sy * TH, x < d.x_max, acc);
+        }
+      }
+      // keep the lane sums in registers (compile-time slots)
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (q == k) {
+          s_k[q] = s;
+#pragma unroll
+          for (int v = 0; v < NVV; v++) tiles[q][v] = acc[v];
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < NVV; v++) {
+      const double t = bfly4(tiles[0][v], tiles[1][v], tiles[2][v], tiles[3][v]);
+      if ((lane & 7) == 0) sh[v * 32 + bfly4_slot(lane) * 8 + warp] = t;
+    }
+    supertile_partials4<NVV>(red, s_k, d.ns, sh);
+  }
+  return finish_reduction<NVV>(red, d.ns, sh);
 }
 
 // True in the last block of the grid to get here (counter reset after).
