@@ -354,17 +354,38 @@ __device__ __forceinline__ void supertile_partials4(const Red& red, const int* s
   __syncthreads();
 }
 
-// Walks the block's supertiles (s = blockIdx.x + j*gridDim.x) four at a
-// time; body(x, y0, xin, acc) processes the TH rows of one lane's column x
+// Walks the block's supertiles (s = blockIdx.x + j*gridDim.x);
+// body(x, y0, xin, acc) processes the TH rows of one lane's column x
 // starting at interior row y0 and adds its contributions row by row into
-// acc[0..NV).  Returns true in the one block that finished the reduction
-// (thread 0 of it holds red.result).
-template <int TH, int NV, class Body>
+// acc[0..NV).  With P = 4 the sums of four supertiles share their
+// butterflies (bfly4, supertile_partials4); with P = 1 every supertile is
+// summed on its own, which needs fewer registers (the FP32 kernels of the
+// mixed solve, held to 32 registers for full occupancy, are faster so).
+// Both give the same bits.  Returns true in the one block that finished
+// the reduction (thread 0 of it holds red.result).
+template <int TH, int NV, class Body, int P = 4>
 __device__ __forceinline__ bool tile_driver(const Dev& d, const Red& red,
                                             Body body) {
   constexpr int NVV = NV > 0 ? NV : 1;
   __shared__ double sh[NVV * 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (NV > 0 && P == 1) {
+    for (int s = blockIdx.x; s < d.ns; s += gridDim.x) {
+      const int sy = s / d.nsx, sx = s - sy * d.nsx;
+      const int tx = sx * kTilesPerSuper + warp;
+      double acc[NVV];
+#pragma unroll
+      for (int v = 0; v < NVV; v++) acc[v] = 0.0;
+      if (tx < d.ntx) {
+        const int x = tx * kTileW + lane;
+        body(x, sy * TH, x < d.x_max, acc);
+#pragma unroll
+        for (int v = 0; v < NVV; v++) acc[v] = bfly(acc[v]);
+      }
+      supertile_partial<NVV>(red, s, acc, sh);
+    }
+    return finish_reduction<NVV>(red, d.ns, sh);
+  }
   if (NV == 0) {
     for (int s = blockIdx.x; s < d.ns; s += gridDim.x) {
       const int sy = s / d.nsx, sx = s - sy * d.nsx;
@@ -411,6 +432,13 @@ __device__ __forceinline__ bool tile_driver(const Dev& d, const Red& red,
     supertile_partials4<NVV>(red, s_k, d.ns, sh);
   }
   return finish_reduction<NVV>(red, d.ns, sh);
+}
+
+// tile_driver summing one supertile at a time (P = 1).
+template <int TH, int NV, class Body>
+__device__ __forceinline__ bool tile_driver_p1(const Dev& d, const Red& red,
+                                               Body body) {
+  return tile_driver<TH, NV, Body, 1>(d, red, body);
 }
 
 // True in the last block of the grid to get here (counter reset after).

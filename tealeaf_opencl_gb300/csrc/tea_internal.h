@@ -181,6 +181,7 @@ struct LaunchCtx {
   int arith;  // arithmetic form
 };
 Dev make_dev_tiling(Dev d);  // fills th, ntx, nsx, nty, ns from x_max, y_max
+Dev rows4_tiling(Dev d);     // the same field set tiled in 4-row tiles
 void dev_volume(const LaunchCtx& l, const Dev& d, double vol);
 void dev_init_common(const LaunchCtx& l, const Dev& d, int coef, double rx,
                      double ry);

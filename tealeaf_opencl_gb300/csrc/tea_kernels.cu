@@ -40,6 +40,46 @@ static void launch_tile(Chunk& c, const char* name, void (*kernel)(KArgs...),
   profile_end(name);
 }
 
+// A kernel that takes no sum computes the same values whatever its tile
+// height, so it may run over 4-row tiles: four times as many, smaller work
+// items as the 16-row tiles of the summing kernels, and no long last wave
+// of blocks (4096 16-row supertiles at 4096^2 make 4.5 rounds of 912
+// blocks).  Measured at 4096^2: update_r 194 -> 191 us, calc_sd 163 -> 159,
+// calc_residual 161 -> 155, calc_p 64.5 -> 62.7, finalise 253 -> 245.
+// Chebyshev calc_p (352 -> 362) and the FP32 calc_p of the mixed solve got
+// slower, so they keep the 16-row tiles.
+Dev rows4_tiling(Dev d) {
+  d.th = 4;
+  d.nty = (d.y_max + 3) / 4;
+  d.ns = d.nsx * d.nty;
+  return d;
+}
+
+static Dev dev4(const Chunk& c) { return rows4_tiling(c.dev()); }
+
+template <class... KArgs, class... Args>
+static void launch_tile_ns(Chunk& c, const char* name, int ns, void (*kernel)(KArgs...),
+                           Args... args) {
+  const long long cap = (long long)c.num_sms * blocks_per_sm((const void*)kernel);
+  const int grid = (int)std::max<long long>(1, std::min<long long>(ns, cap));
+  profile_begin(name);
+  kernel<<<grid, kBlock, 0, c.stream>>>(args...);
+  count_launch(name);
+  check_cuda(cudaGetLastError(), name);
+  profile_end(name);
+}
+
+// TH_DISPATCH for kernels that take no sum: 4-row tiles (dev4)
+#define TH4_DISPATCH(c, name, kern, d4, ...)                           \
+  do {                                                                 \
+    if ((c).arith == 2)                                                \
+      launch_tile_ns(c, name, (d4).ns, kern<4, 2>, d4, __VA_ARGS__);   \
+    else if ((c).arith == 1)                                           \
+      launch_tile_ns(c, name, (d4).ns, kern<4, 1>, d4, __VA_ARGS__);   \
+    else                                                               \
+      launch_tile_ns(c, name, (d4).ns, kern<4, 0>, d4, __VA_ARGS__);   \
+  } while (0)
+
 template <class... KArgs, class... Args>
 static void launch_2d(Chunk& c, const char* name, int nx, int ny,
                       void (*kernel)(KArgs...), Args... args) {
@@ -807,7 +847,7 @@ void launch_zero_boundary(Chunk& c, const int* zb) {
 }
 
 void launch_calc_residual(Chunk& c) {
-  TH_DISPATCH(c, "tea_leaf_calc_residual", k_calc_residual, c.dev(), c.red());
+  TH4_DISPATCH(c, "tea_leaf_calc_residual", k_calc_residual, dev4(c), c.red());
 }
 
 void launch_dot(Chunk& c, const double* a, const double* b) {
@@ -844,7 +884,7 @@ void launch_cg_calc_ur(Chunk& c, double alpha) {
 }
 
 void launch_cg_calc_p(Chunk& c, double beta) {
-  TH_DISPATCH(c, "tea_leaf_cg_solve_calc_p", k_cg_calc_p, c.dev(), c.red(), beta,
+  TH4_DISPATCH(c, "tea_leaf_cg_solve_calc_p", k_cg_calc_p, dev4(c), c.red(), beta,
               (ResState*)nullptr, (unsigned int*)nullptr);
 }
 
@@ -859,26 +899,26 @@ void launch_cheby_calc_p(Chunk& c, double alpha, double beta) {
 }
 
 void launch_cheby_calc_u(Chunk& c) {
-  TH_DISPATCH(c, "tea_leaf_cheby_solve_calc_u", k_cheby_calc_u, c.dev(), c.red());
+  TH4_DISPATCH(c, "tea_leaf_cheby_solve_calc_u", k_cheby_calc_u, dev4(c), c.red());
 }
 
 void launch_ppcg_init_sd(Chunk& c, double theta) {
-  TH_DISPATCH(c, "tea_leaf_ppcg_solve_init_sd", k_ppcg_sd, c.dev(), c.red(), 0,
+  TH4_DISPATCH(c, "tea_leaf_ppcg_solve_init_sd", k_ppcg_sd, dev4(c), c.red(), 0,
               theta, 0.0, 0.0, (const ResState*)nullptr);
 }
 
 void launch_ppcg_update_r(Chunk& c) {
-  TH_DISPATCH(c, "tea_leaf_ppcg_solve_update_r", k_ppcg_update_r, c.dev(),
+  TH4_DISPATCH(c, "tea_leaf_ppcg_solve_update_r", k_ppcg_update_r, dev4(c),
               c.red(), (const ResState*)nullptr);
 }
 
 void launch_ppcg_calc_sd(Chunk& c, double alpha, double beta) {
-  TH_DISPATCH(c, "tea_leaf_ppcg_solve_calc_sd", k_ppcg_sd, c.dev(), c.red(), 1,
+  TH4_DISPATCH(c, "tea_leaf_ppcg_solve_calc_sd", k_ppcg_sd, dev4(c), c.red(), 1,
               0.0, alpha, beta, (const ResState*)nullptr);
 }
 
 void launch_jacobi_copy_u(Chunk& c) {
-  TH_DISPATCH(c, "tea_leaf_jacobi_copy_u", k_jacobi_copy_u, c.dev(), c.red());
+  TH4_DISPATCH(c, "tea_leaf_jacobi_copy_u", k_jacobi_copy_u, dev4(c), c.red());
 }
 
 void launch_jacobi_solve(Chunk& c) {
@@ -886,7 +926,7 @@ void launch_jacobi_solve(Chunk& c) {
 }
 
 void launch_finalise(Chunk& c) {
-  TH_DISPATCH(c, "tea_leaf_finalise", k_finalise, c.dev(), c.red());
+  TH4_DISPATCH(c, "tea_leaf_finalise", k_finalise, dev4(c), c.red());
 }
 
 void launch_field_summary(Chunk& c) {
@@ -1014,9 +1054,9 @@ void dev_field_summary(const LaunchCtx& l, const Dev& d, const Red& r) {
 // Grid size of a tile kernel: every SM filled once, capped by the number of
 // supertiles.
 template <class... KArgs>
-static int tile_grid(Chunk& c, void (*kernel)(KArgs...)) {
+static int tile_grid(Chunk& c, void (*kernel)(KArgs...), int ns = 0) {
   const long long cap = (long long)c.num_sms * blocks_per_sm((const void*)kernel);
-  return (int)std::max<long long>(1, std::min<long long>(c.dev().ns, cap));
+  return (int)std::max<long long>(1, std::min<long long>(ns > 0 ? ns : c.dev().ns, cap));
 }
 
 // The whole remaining CG loop as one cooperative launch, for grids whose
@@ -1148,25 +1188,26 @@ __global__ void __launch_bounds__(kBlock) k_ppcg_rz_step(Dev d, Red red, ResStat
 template <int TH, int F>
 static void enqueue_ppcg_iterations_t(Chunk& c, int iters) {
   const Dev d = c.dev();
+  const Dev d4 = dev4(c);  // the kernels that take no sum
   const Red red = c.red();
   ResState* st = c.res_state;
   const double theta = c.ppcg_theta;
   const int gw = tile_grid(c, k_cg_calc_w<TH, F>);
   const int gu = tile_grid(c, k_ppcg_ur_sd<TH, F>);
-  const int gr = tile_grid(c, k_ppcg_update_r<TH, F>);
-  const int gs = tile_grid(c, k_ppcg_sd<TH, F>);
+  const int gr = tile_grid(c, k_ppcg_update_r<4, F>, d4.ns);
+  const int gs = tile_grid(c, k_ppcg_sd<4, F>, d4.ns);
   const int gz = tile_grid(c, k_ppcg_rz_step<TH, F>);
-  const int gp = tile_grid(c, k_cg_calc_p<TH, F>);
+  const int gp = tile_grid(c, k_cg_calc_p<4, F>, d4.ns);
   for (int i = 0; i < iters; i++) {
     k_cg_calc_w<TH, F><<<gw, kBlock, 0, c.stream>>>(d, red, st);
     k_ppcg_ur_sd<TH, F><<<gu, kBlock, 0, c.stream>>>(d, red, st, theta);
     for (int k = 0; k < c.n_ppcg; k++) {
-      k_ppcg_update_r<TH, F><<<gr, kBlock, 0, c.stream>>>(d, red, st);
-      k_ppcg_sd<TH, F><<<gs, kBlock, 0, c.stream>>>(d, red, 1, 0.0, c.ppcg_alpha_h[k],
-                                                    c.ppcg_beta_h[k], st);
+      k_ppcg_update_r<4, F><<<gr, kBlock, 0, c.stream>>>(d4, red, st);
+      k_ppcg_sd<4, F><<<gs, kBlock, 0, c.stream>>>(d4, red, 1, 0.0, c.ppcg_alpha_h[k],
+                                                   c.ppcg_beta_h[k], st);
     }
     k_ppcg_rz_step<TH, F><<<gz, kBlock, 0, c.stream>>>(d, red, st);
-    k_cg_calc_p<TH, F><<<gp, kBlock, 0, c.stream>>>(d, red, 0.0, st, c.res_counter);
+    k_cg_calc_p<4, F><<<gp, kBlock, 0, c.stream>>>(d4, red, 0.0, st, c.res_counter);
   }
 }
 
@@ -1185,15 +1226,16 @@ static void enqueue_ppcg_iterations(Chunk& c, int iters) {
 template <int TH, int F, int NV>
 static void enqueue_resident_iterations_t(Chunk& c, int iters) {
   const Dev d = c.dev();
+  const Dev d4 = dev4(c);  // calc_p takes no sum
   const Red red = c.red();
   const int gw = tile_grid(c, k_cg_calc_w<TH, F>);
   const int gu = tile_grid(c, k_cg_calc_ur<TH, F, NV>);
-  const int gp = tile_grid(c, k_cg_calc_p<TH, F>);
+  const int gp = tile_grid(c, k_cg_calc_p<4, F>, d4.ns);
   for (int i = 0; i < iters; i++) {
     k_cg_calc_w<TH, F><<<gw, kBlock, 0, c.stream>>>(d, red, c.res_state);
     k_cg_calc_ur<TH, F, NV><<<gu, kBlock, 0, c.stream>>>(d, red, 0.0, c.res_state);
-    k_cg_calc_p<TH, F><<<gp, kBlock, 0, c.stream>>>(d, red, 0.0, c.res_state,
-                                                    c.res_counter);
+    k_cg_calc_p<4, F><<<gp, kBlock, 0, c.stream>>>(d4, red, 0.0, c.res_state,
+                                                   c.res_counter);
   }
 }
 

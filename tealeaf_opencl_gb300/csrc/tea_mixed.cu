@@ -131,7 +131,7 @@ __global__ void k_mix_convert(Dev d, MixDev m) {
 template <int TH>
 __global__ void __launch_bounds__(kBlock)
     k_mix_residual(Dev d, MixDev m, Red red) {
-  tile_driver<TH, 2>(d, red, [&](int x, int y0, bool xin, double* acc) {
+  tile_driver_p1<TH, 2>(d, red, [&](int x, int y0, bool xin, double* acc) {
     float hi = 0.0f, lo = 0.0f;
 #pragma unroll 1
     for (int g = y0; g < y0 + TH; g += 4) {
@@ -170,7 +170,7 @@ template <int TH>
 __global__ void __launch_bounds__(kBlock, kMixMinBlocks)
     k_mix_calc_w(Dev d, MixDev m, Red red, MixState* st) {
   if (*(volatile int*)&st->stop) return;
-  const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+  const bool last = tile_driver_p1<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
     float hi = 0.0f, lo = 0.0f;
     constexpr int GR = kGroup<TH>;
 #pragma unroll 1
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(kBlock, kMixMinBlocks)
   if (*(volatile int*)&st->stop) return;
   const double alpha = st->rro / st->pw;
   const float af = (float)alpha;
-  const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+  const bool last = tile_driver_p1<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
     float hi = 0.0f, lo = 0.0f;
     constexpr int GR = kGroup<TH>;
 #pragma unroll 1
@@ -360,7 +360,7 @@ template <int TH>
 __global__ void __launch_bounds__(kBlock, kMixMinBlocks)
     k_mix_ppcg_rz(Dev d, MixDev m, Red red, MixState* st) {
   if (*(volatile int*)&st->stop) return;
-  const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+  const bool last = tile_driver_p1<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
     float hi = 0.0f, lo = 0.0f;
 #pragma unroll 4
     for (int j = 0; j < TH; j++) {
@@ -430,14 +430,14 @@ __global__ void __launch_bounds__(kBlock) k_mix_update_u(Dev d, MixDev m, Red re
 }
 
 template <class... KArgs>
-static int mix_grid(Chunk& c, void (*kernel)(KArgs...)) {
+static int mix_grid(Chunk& c, void (*kernel)(KArgs...), int ns = 0) {
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, (const void*)kernel, kBlock, 0) !=
           cudaSuccess ||
       n < 1)
     n = 1;
   const long long cap = (long long)c.num_sms * n;
-  return (int)std::max<long long>(1, std::min<long long>(c.dev().ns, cap));
+  return (int)std::max<long long>(1, std::min<long long>(ns > 0 ? ns : c.dev().ns, cap));
 }
 
 template <int TH>
