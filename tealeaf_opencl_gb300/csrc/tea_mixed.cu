@@ -66,11 +66,11 @@ struct MixChunk {
 
 static MixChunk g_mix;
 
-// Rows per load group of the FP32 iteration kernels, and their minimum
-// resident blocks per SM.  Measured at 4096^2 (ms per inner iteration):
-// groups of 1/2/4/8 rows at 8 blocks/SM (32 registers) 0.229/0.240/0.252/-,
-// groups of 4 or 8 rows without the bound 0.277/0.303.  Occupancy is what
-// keeps these HBM-bound kernels fed.
+// Rows per load group of the one-column FP32 kernels (k_mix_calc_w and the
+// PPCG kernels), and their minimum resident blocks per SM.  Measured at
+// 4096^2 (ms per CG inner iteration, before the 4-column kernels below):
+// groups of 1/2/4 rows at 8 blocks/SM (32 registers) 0.229/0.240/0.252,
+// groups of 4 or 8 rows without the bound 0.277/0.303.
 template <int TH>
 constexpr int kGroup = 1;
 constexpr int kMixMinBlocks = 8;
@@ -196,41 +196,161 @@ __global__ void __launch_bounds__(kBlock, kMixMinBlocks)
   if (last && threadIdx.x == 0) st->pw = red.result[0];
 }
 
-// alpha = rro/pw; d += alpha p; r -= alpha w; z = Mi r; sum r.z; the last
-// block takes the CG scalar step and the inner exit test
+// ---- FP32 iteration kernels with 16-byte accesses ----
+//
+// One-column FP32 kernels put 4 bytes per lane into every memory request,
+// half of FP64's, and ran at about 70 % of HBM.  With float4 accesses the
+// CG inner iteration at 4096^2 went from 0.229 ms to 0.217 ms (calc_p)
+// and 0.197 ms (calc_w and calc_ur too); 4 blocks per SM measured best
+// (5 and 6: 0.210 and 0.220 ms).
+//
+// Every thread takes 4 adjacent columns (one float4) of one tile; 8 threads
+// cover a tile's 32 columns and 64 threads a supertile, so a 256-thread
+// block works on 4 supertiles (s0 + k*gridDim.x, k = 0..3) at once.  Each
+// column's lane sum is accumulated exactly as in the one-column kernels.
+// The tile's xor butterfly over its 32 columns runs on 4 values per
+// thread: the stages xor 16, 8, 4 become shuffles xor 4, 2, 1 between the
+// tile's 8 threads, and the stages xor 2, 1 happen within a thread.  Every
+// stage adds the same pairs, so the sums are bit-identical.
+
+__device__ __forceinline__ float4 ld4(const float* p) {
+  return *reinterpret_cast<const float4*>(p);
+}
+__device__ __forceinline__ float f4(const float4& v, int k) {
+  return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
+}
+
+// Walks 4 supertiles per block and round; body(x, y0, v) gives v[k], the
+// lane sum of interior column x+k of the tile rows y0..y0+TH-1 (0.0 for
+// columns past the interior).  Forms the supertile partials and finishes
+// the reduction in the last block (thread 0 of it holds red.result).
+template <int TH, class Body>
+__device__ __forceinline__ bool quad_driver(const Dev& d, const Red& red, Body body) {
+  __shared__ double sh[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int grp = warp >> 1;                       // supertile slot
+  const int tile = 4 * (warp & 1) + (lane >> 3);   // tile within the supertile
+  const int q = lane & 7;                          // column quad within the tile
+  for (int s0 = blockIdx.x; s0 < d.ns; s0 += 4 * gridDim.x) {
+    const int s = s0 + grp * gridDim.x;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    if (s < d.ns) {
+      const int sy = s / d.nsx, sx = s - sy * d.nsx;
+      const int tx = sx * kTilesPerSuper + tile;
+      if (tx < d.ntx) body(tx * kTileW + 4 * q, sy * TH, v);
+    }
+#pragma unroll
+    for (int off = 4; off >= 1; off >>= 1) {
+#pragma unroll
+      for (int k = 0; k < 4; k++) v[k] = v[k] + __shfl_xor_sync(0xffffffffu, v[k], off);
+    }
+    const double t = (v[0] + v[2]) + (v[1] + v[3]);
+    if (q == 0) sh[grp * 8 + tile] = t;
+    int s_k[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) s_k[k] = s0 + k * gridDim.x;
+    supertile_partials4<1>(red, s_k, d.ns, sh);
+  }
+  return finish_reduction<1>(red, d.ns, sh);
+}
+
+// w = A p and p.w (k_mix_calc_w's values), 4 columns per thread
 template <int TH>
-__global__ void __launch_bounds__(kBlock, kMixMinBlocks)
-    k_mix_calc_ur(Dev d, MixDev m, Red red, MixState* st) {
+__global__ void __launch_bounds__(kBlock, 4)
+    k_mix_calc_w4(Dev d, MixDev m, Red red, MixState* st) {
+  if (*(volatile int*)&st->stop) return;
+  const bool last = quad_driver<TH>(d, red, [&](int x, int y0, double* v) {
+    const long long S = m.S;
+    float hi[4] = {0.0f, 0.0f, 0.0f, 0.0f}, lo[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const bool full = x + 4 <= d.x_max;
+#pragma unroll 1
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      float pv[4] = {0.0f, 0.0f, 0.0f, 0.0f}, wv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      if (y < d.y_max) {
+        const long long c = cidx32(d, m, x, y);
+        if (full) {
+          const float4 pc = ld4(m.p + c), pn = ld4(m.p + c + S), ps = ld4(m.p + c - S);
+          const float4 kx = ld4(m.Kx + c), kyc = ld4(m.Ky + c), kyn = ld4(m.Ky + c + S);
+          const float4 D = ld4(m.D + c);
+          const float pwst = m.p[c - 1], peas = m.p[c + 4], kx4 = m.Kx[c + 4];
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            const float xw = k == 0 ? pwst : f4(pc, k - 1);
+            const float xe = k == 3 ? peas : f4(pc, k + 1);
+            const float ke = k == 3 ? kx4 : f4(kx, k + 1);
+            const float t1 = __fmaf_rn(f4(kyc, k), f4(ps, k), f4(kyn, k) * f4(pn, k));
+            const float t2 = __fmaf_rn(f4(kx, k), xw, ke * xe);
+            wv[k] = __fmaf_rn(f4(D, k), f4(pc, k), -t1) - t2;
+            pv[k] = f4(pc, k);
+          }
+          *reinterpret_cast<float4*>(m.w + c) = make_float4(wv[0], wv[1], wv[2], wv[3]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; k++)
+            if (x + k < d.x_max) {
+              wv[k] = smvp32(m, m.p, c + k);
+              pv[k] = m.p[c + k];
+              m.w[c + k] = wv[k];
+            }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 4; k++) acc_pair(hi[k], lo[k], pv[k], wv[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) v[k] = pair_value(hi[k], lo[k]);
+  });
+  if (last && threadIdx.x == 0) st->pw = red.result[0];
+}
+
+// d += alpha p; r -= alpha w; z = Mi r; r.z and the inner loop's scalar
+// step (k_mix_calc_ur's values), 4 columns per thread
+template <int TH>
+__global__ void __launch_bounds__(kBlock, 4)
+    k_mix_calc_ur4(Dev d, MixDev m, Red red, MixState* st) {
   if (*(volatile int*)&st->stop) return;
   const double alpha = st->rro / st->pw;
   const float af = (float)alpha;
-  const bool last = tile_driver_p1<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
-    float hi = 0.0f, lo = 0.0f;
-    constexpr int GR = kGroup<TH>;
+  const bool last = quad_driver<TH>(d, red, [&](int x, int y0, double* v) {
+    float hi[4] = {0.0f, 0.0f, 0.0f, 0.0f}, lo[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const bool full = x + 4 <= d.x_max;
 #pragma unroll 1
-    for (int g = y0; g < y0 + TH; g += GR) {
-      float dv[GR], rv[GR], zv[GR];
+    for (int j = 0; j < TH; j++) {
+      const int y = y0 + j;
+      float rv[4] = {0.0f, 0.0f, 0.0f, 0.0f}, zv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      if (y < d.y_max) {
+        const long long c = cidx32(d, m, x, y);
+        if (full) {
+          const float4 p4 = ld4(m.p + c), d4 = ld4(m.d + c), w4 = ld4(m.w + c);
+          const float4 r4 = ld4(m.r + c), mi4 = ld4(m.Mi + c);
+          float dv[4];
 #pragma unroll
-      for (int j = 0; j < GR; j++) {
-        dv[j] = rv[j] = zv[j] = 0.0f;
-        if (xin && g + j < d.y_max) {
-          const long long c3 = cidx32(d, m, x, g + j);
-          dv[j] = __fmaf_rn(af, m.p[c3], m.d[c3]);
-          rv[j] = __fmaf_rn(-af, m.w[c3], m.r[c3]);
-          zv[j] = m.Mi[c3] * rv[j];
+          for (int k = 0; k < 4; k++) {
+            dv[k] = __fmaf_rn(af, f4(p4, k), f4(d4, k));
+            rv[k] = __fmaf_rn(-af, f4(w4, k), f4(r4, k));
+            zv[k] = f4(mi4, k) * rv[k];
+          }
+          *reinterpret_cast<float4*>(m.d + c) = make_float4(dv[0], dv[1], dv[2], dv[3]);
+          *reinterpret_cast<float4*>(m.r + c) = make_float4(rv[0], rv[1], rv[2], rv[3]);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; k++)
+            if (x + k < d.x_max) {
+              const long long ck = c + k;
+              const float dk = __fmaf_rn(af, m.p[ck], m.d[ck]);
+              rv[k] = __fmaf_rn(-af, m.w[ck], m.r[ck]);
+              zv[k] = m.Mi[ck] * rv[k];
+              m.d[ck] = dk;
+              m.r[ck] = rv[k];
+            }
         }
       }
 #pragma unroll
-      for (int j = 0; j < GR; j++) {
-        if (xin && g + j < d.y_max) {
-          const long long c3 = cidx32(d, m, x, g + j);
-          m.d[c3] = dv[j];
-          m.r[c3] = rv[j];
-        }
-        acc_pair(hi, lo, rv[j], zv[j]);
-      }
+      for (int k = 0; k < 4; k++) acc_pair(hi[k], lo[k], rv[k], zv[k]);
     }
-    acc[0] = pair_value(hi, lo);
+#pragma unroll
+    for (int k = 0; k < 4; k++) v[k] = pair_value(hi[k], lo[k]);
   });
   if (last && threadIdx.x == 0) {
     const double rrn = red.result[0];
@@ -252,26 +372,46 @@ __global__ void __launch_bounds__(kBlock, kMixMinBlocks)
   }
 }
 
-// p = Mi r + beta p
-template <int TH>
-__global__ void __launch_bounds__(kBlock, kMixMinBlocks)
-    k_mix_calc_p(Dev d, MixDev m, Red red, MixState* st, unsigned int* counter) {
+// p = Mi r + beta p with 16-byte loads: each thread updates 4 adjacent
+// columns of 8 rows.  FP32 loads of 4 bytes per lane put half the bytes of
+// FP64 into every memory request; float4 requests carry 16 bytes per lane.
+// The values are those of k_mix_calc_p (the same fused multiply-add per
+// cell).  Interior column 0 of every row is 256-byte aligned.
+__global__ void __launch_bounds__(kBlock)
+    k_mix_calc_p_v4(Dev d, MixDev m, MixState* st, unsigned int* counter) {
   if (!*(volatile int*)&st->p_pending) return;
   const float bf = (float)st->beta;
-  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
-    if (!xin) return;
-    float pv[TH];
+  const int nq = (d.x_max + 3) / 4, ng = (d.y_max + 7) / 8;
+  const long long items = (long long)nq * ng;
+  for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < items;
+       it += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(it % nq), g = (int)(it / nq);
+    const int x = 4 * q, y0 = 8 * g;
+    const int rows = min(8, d.y_max - y0);
+    if (x + 4 <= d.x_max) {
+      float4 pv[8];
 #pragma unroll
-    for (int j = 0; j < TH; j++) {
-      if (y0 + j < d.y_max) {
-        const long long c3 = cidx32(d, m, x, y0 + j);
-        pv[j] = __fmaf_rn(bf, m.p[c3], m.Mi[c3] * m.r[c3]);
+      for (int j = 0; j < 8; j++) {
+        if (j < rows) {
+          const long long c3 = cidx32(d, m, x, y0 + j);
+          const float4 p4 = *reinterpret_cast<const float4*>(m.p + c3);
+          const float4 m4 = *reinterpret_cast<const float4*>(m.Mi + c3);
+          const float4 r4 = *reinterpret_cast<const float4*>(m.r + c3);
+          pv[j] = make_float4(__fmaf_rn(bf, p4.x, m4.x * r4.x), __fmaf_rn(bf, p4.y, m4.y * r4.y),
+                              __fmaf_rn(bf, p4.z, m4.z * r4.z), __fmaf_rn(bf, p4.w, m4.w * r4.w));
+        }
       }
-    }
 #pragma unroll
-    for (int j = 0; j < TH; j++)
-      if (y0 + j < d.y_max) m.p[cidx32(d, m, x, y0 + j)] = pv[j];
-  });
+      for (int j = 0; j < 8; j++)
+        if (j < rows) *reinterpret_cast<float4*>(m.p + cidx32(d, m, x, y0 + j)) = pv[j];
+    } else {
+      for (int j = 0; j < rows; j++)
+        for (int k = x; k < d.x_max; k++) {
+          const long long c3 = cidx32(d, m, k, y0 + j);
+          m.p[c3] = __fmaf_rn(bf, m.p[c3], m.Mi[c3] * m.r[c3]);
+        }
+    }
+  }
   if (last_block(counter) && threadIdx.x == 0) {
     st->p_pending = 0;
     __threadfence();
@@ -445,13 +585,17 @@ static void enqueue_inner(Chunk& c, int iters) {
   const Dev d = c.dev();
   const Red red = c.red();
   const MixDev m = g_mix.dev;
-  const int gw = mix_grid(c, k_mix_calc_w<TH>);
-  const int gu = mix_grid(c, k_mix_calc_ur<TH>);
-  const int gp = mix_grid(c, k_mix_calc_p<TH>);
+  const int nblk4 = (d.ns + 3) / 4;  // 4 supertiles per block and round
+  const int gw = mix_grid(c, k_mix_calc_w4<TH>, nblk4);
+  const int gu = mix_grid(c, k_mix_calc_ur4<TH>, nblk4);
+  const int gp = mix_grid(c, k_mix_calc_p_v4,
+                          (int)std::min<long long>(1 << 30, ((long long)(d.x_max + 3) / 4 *
+                                                             ((d.y_max + 7) / 8) + kBlock - 1) /
+                                                                kBlock));
   for (int i = 0; i < iters; i++) {
-    k_mix_calc_w<TH><<<gw, kBlock, 0, c.stream>>>(d, m, red, g_mix.st);
-    k_mix_calc_ur<TH><<<gu, kBlock, 0, c.stream>>>(d, m, red, g_mix.st);
-    k_mix_calc_p<TH><<<gp, kBlock, 0, c.stream>>>(d, m, red, g_mix.st, g_mix.counter);
+    k_mix_calc_w4<TH><<<gw, kBlock, 0, c.stream>>>(d, m, red, g_mix.st);
+    k_mix_calc_ur4<TH><<<gu, kBlock, 0, c.stream>>>(d, m, red, g_mix.st);
+    k_mix_calc_p_v4<<<gp, kBlock, 0, c.stream>>>(d, m, g_mix.st, g_mix.counter);
   }
 }
 
