@@ -41,6 +41,7 @@
 // kernels, and the fused form roughly halves their FP64 instruction count.
 #pragma once
 
+#include "tea_emu.cuh"
 #include "tea_internal.h"
 
 namespace tea {
@@ -69,7 +70,22 @@ __device__ __forceinline__ double ldv(const double* p) {
   return CG ? __ldcg(p) : *p;
 }
 
-template <int F, bool CG = false>
+// a * b on the FP64 pipe or, with EMU, on the integer pipes (tea_emu.cuh):
+// the same bits either way.
+template <bool EMU>
+__device__ __forceinline__ double mul_e(double a, double b) {
+  return EMU ? emu_dmul(a, b) : a * b;
+}
+
+// A x at offset c.  With EMU some products run on the integer pipes (the
+// one that starts the chain form, the two that feed no fused multiply-add
+// in the fused form, two of the five in the exact form):
+// GB300's FP64 pipe bounds the kernels that apply the operator, and moving
+// those products off it took calc_w from 206 to 186 us (chain) and from 251
+// to 214 us (fused) at 4096^2.  Kernels with high register pressure (the
+// Chebyshev step) keep EMU off: the extra registers cost them more than the
+// FP64 instructions saved.
+template <int F, bool CG = false, bool EMU = true>
 __device__ __forceinline__ double smvp(const Dev& d, const double* x,
                                        long long c) {
   const long long S = d.S;
@@ -77,17 +93,18 @@ __device__ __forceinline__ double smvp(const Dev& d, const double* x,
   const double kxe = __ldg(d.Kx + c + 1), kxc = __ldg(d.Kx + c);
   const double D = __ldg(d.diag + c);
   if (!F)
-    return D * ldv<CG>(x + c) - (kyn * ldv<CG>(x + c + S) + kyc * ldv<CG>(x + c - S)) -
-           (kxe * ldv<CG>(x + c + 1) + kxc * ldv<CG>(x + c - 1));
+    return D * ldv<CG>(x + c) -
+           (mul_e<EMU>(kyn, ldv<CG>(x + c + S)) + kyc * ldv<CG>(x + c - S)) -
+           (mul_e<EMU>(kxe, ldv<CG>(x + c + 1)) + kxc * ldv<CG>(x + c - 1));
   if (F == 2) {
-    double t = D * ldv<CG>(x + c);
+    double t = mul_e<EMU>(D, ldv<CG>(x + c));
     t = __fma_rn(-kyn, ldv<CG>(x + c + S), t);
     t = __fma_rn(-kyc, ldv<CG>(x + c - S), t);
     t = __fma_rn(-kxe, ldv<CG>(x + c + 1), t);
     return __fma_rn(-kxc, ldv<CG>(x + c - 1), t);
   }
-  const double t1 = __fma_rn(kyc, ldv<CG>(x + c - S), kyn * ldv<CG>(x + c + S));
-  const double t2 = __fma_rn(kxc, ldv<CG>(x + c - 1), kxe * ldv<CG>(x + c + 1));
+  const double t1 = __fma_rn(kyc, ldv<CG>(x + c - S), mul_e<EMU>(kyn, ldv<CG>(x + c + S)));
+  const double t2 = __fma_rn(kxc, ldv<CG>(x + c - 1), mul_e<EMU>(kxe, ldv<CG>(x + c + 1)));
   return __fma_rn(D, ldv<CG>(x + c), -t1) - t2;
 }
 

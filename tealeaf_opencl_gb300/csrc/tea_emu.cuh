@@ -1,0 +1,86 @@
+// Correctly rounded FP64 add and multiply on the integer pipes.
+//
+// GB300 issues about two FP64 lanes per clock per SM, against 128 lanes of
+// 32-bit integer and FP32 work, so every stencil kernel of the solve waits
+// on its FP64 instructions while most issue slots stay empty.  These
+// functions compute IEEE 754 binary64 addition and multiplication with
+// round-to-nearest-even from the operands' bit patterns, using only integer
+// instructions, so a kernel can move part of its FP64 work off the FP64
+// pipe and still produce the hardware's results bit for bit.
+//
+// Method (textbook IEEE arithmetic, e.g. the sum and product algorithms in
+// Muller et al., Handbook of Floating-Point Arithmetic, ch. 7-8): align the
+// significands in 64-bit integers with guard bits and a sticky bit, add or
+// multiply exactly, normalise, round to nearest even on the guard bits.
+// Operands or results outside the normal range (zeros, subnormals,
+// infinities, NaNs, overflow, underflow) take the hardware instruction
+// instead, so those cases are the hardware's by construction.
+#pragma once
+
+#include <stdint.h>
+
+namespace tea {
+
+constexpr uint64_t kSign = 0x8000000000000000ull;
+constexpr uint64_t kFrac = 0x000fffffffffffffull;
+constexpr uint64_t kHidden = 0x0010000000000000ull;
+
+// Round the 64-bit significand f (leading one at bit 63) to 53 bits with
+// sticky information s below bit 0 and pack it with biased exponent e and
+// sign bit sg, as a bit pattern.  A carry out of the rounding moves into
+// the exponent field.
+__device__ __forceinline__ uint64_t emu_pack(uint64_t sg, int e, uint64_t f, bool s) {
+  uint64_t m = f >> 11;
+  const uint32_t rest = (uint32_t)f & 0x7ffu;
+  m += (rest > 0x400u || (rest == 0x400u && (s || (m & 1)))) ? 1 : 0;
+  return sg + ((uint64_t)(e - 1) << 52) + m;
+}
+
+// a + b, rounded to nearest even.
+__device__ __forceinline__ double emu_dadd(double a, double b) {
+  const uint64_t ia = (uint64_t)__double_as_longlong(a);
+  const uint64_t ib = (uint64_t)__double_as_longlong(b);
+  const bool swap = (ia & ~kSign) < (ib & ~kSign);
+  const uint64_t x = swap ? ib : ia;  // larger magnitude
+  const uint64_t y = swap ? ia : ib;
+  const int ex = (int)(x >> 52) & 0x7ff, ey = (int)(y >> 52) & 0x7ff;
+  // With ex >= 64 even total cancellation (at most 63 leading zeros) leaves
+  // a normal result, so every case for the hardware is known here.
+  if (ex < 64 || ex >= 0x7fe || ey == 0) return __dadd_rn(a, b);
+  const uint64_t fx = ((x & kFrac) | kHidden) << 10;  // leading one at bit 62
+  uint64_t fy = ((y & kFrac) | kHidden) << 10;
+  const int d = ex - ey;
+  if (d >= 64) {
+    fy = 1;  // only the sticky bit is left
+  } else if (d > 0) {
+    const uint64_t lost = fy << (64 - d);
+    fy = (fy >> d) | (lost != 0 ? 1 : 0);
+  }
+  const uint64_t f = ((x ^ y) & kSign) ? fx - fy : fx + fy;
+  // Exact cancellation gives +0.  The zero is selected as a bit pattern:
+  // a floating-point select would go through the FP64 pipe.
+  const uint64_t fs = f | (f == 0 ? 1 : 0);
+  const int lz = __clzll((long long)fs);  // 0 after a carry, 1, or more after cancellation
+  const uint64_t r = emu_pack(x & kSign, ex + 1 - lz, fs << lz, false);
+  return __longlong_as_double((long long)(f == 0 ? 0 : r));
+}
+
+// a * b, rounded to nearest even.
+__device__ __forceinline__ double emu_dmul(double a, double b) {
+  const uint64_t ia = (uint64_t)__double_as_longlong(a);
+  const uint64_t ib = (uint64_t)__double_as_longlong(b);
+  const int ea = (int)(ia >> 52) & 0x7ff, eb = (int)(ib >> 52) & 0x7ff;
+  const int e0 = ea + eb - 1023;  // biased exponent of a product in [1, 2)
+  if (ea == 0 || eb == 0 || ea == 0x7ff || eb == 0x7ff || e0 < 1 || e0 > 0x7fd)
+    return __dmul_rn(a, b);
+  const uint64_t ma = ((ia & kFrac) | kHidden) << 11;  // [2^63, 2^64)
+  const uint64_t mb = ((ib & kFrac) | kHidden) << 11;
+  const uint64_t hi = __umul64hi(ma, mb);  // product in [2^126, 2^128)
+  const uint64_t lo = ma * mb;
+  const int top = (int)(hi >> 63);  // 1 when the product is in [2, 4)
+  const uint64_t f = top ? hi : ((hi << 1) | (lo >> 63));
+  const uint64_t below = top ? lo : (lo << 1);
+  return __longlong_as_double((long long)emu_pack((ia ^ ib) & kSign, e0 + top, f, below != 0));
+}
+
+}  // namespace tea

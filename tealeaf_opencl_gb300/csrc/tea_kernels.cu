@@ -500,7 +500,7 @@ __global__ void __launch_bounds__(kBlock)
         for (int i = 0; i < 4; i++) {
           if (ys + i < d.y_max) {
             const long long c = c0 + i * d.S;
-            wl[i] = smvp<F>(d, d.u, c);
+            wl[i] = smvp<F, false, false>(d, d.u, c);
             rl[i] = d.u0[c] - wl[i];
             if (mode != 0) pl[i] = d.p[c];
           }
@@ -533,7 +533,7 @@ __global__ void __launch_bounds__(kBlock)
         for (int j = 0; j < 4; j++) {
           if (g + j < d.y_max) {
             const long long c = c0 + j * d.S;
-            const double wv = smvp<F>(d, d.u, c);
+            const double wv = smvp<F, false, false>(d, d.u, c);
             const double rv = d.u0[c] - wv;
             wl[j] = wv;
             rl[j] = rv;

@@ -1,0 +1,84 @@
+"""The integer FP64 add and multiply (tea_emu.cuh) against IEEE arithmetic.
+
+The stencil kernels move part of their FP64 adds and multiplies to integer
+instructions; the solve stays bit-exact only if those give the correctly
+rounded result for every operand pair.  The header is built for the host
+here and compared bit for bit with numpy's float64 + and * on random
+operands over the whole exponent range, on the hard cases of each
+algorithm (cancellation, exact ties, carries out of the rounding) and on
+zeros, subnormals, infinities and NaNs (which take the fallback).
+"""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(os.path.dirname(HERE), "tealeaf_opencl_gb300", "csrc")
+P = ctypes.POINTER(ctypes.c_double)
+
+
+@pytest.fixture(scope="module")
+def emu(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    out = str(tmp_path_factory.mktemp("emu") / "emu.so")
+    subprocess.run([cxx, "-O2", "-ffp-contract=off", "-shared", "-fPIC", "-I", CSRC,
+                    os.path.join(HERE, "native", "emu_harness.cpp"), "-o", out], check=True)
+    return ctypes.CDLL(out)
+
+
+def call(fn, a, b):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    o = np.empty_like(a)
+    fn(a.ctypes.data_as(P), b.ctypes.data_as(P), o.ctypes.data_as(P), ctypes.c_long(a.size))
+    return o
+
+
+def mismatches(want, got):
+    both_nan = np.isnan(want) & np.isnan(got)
+    return int(np.sum((want.view(np.uint64) != got.view(np.uint64)) & ~both_nan))
+
+
+def rand_bits(rng, n, elo, ehi, low_zero_bits=0):
+    s = rng.integers(0, 2, n, dtype=np.uint64) << np.uint64(63)
+    e = rng.integers(elo, ehi + 1, n, dtype=np.uint64) << np.uint64(52)
+    m = rng.integers(0, 1 << 52, n, dtype=np.uint64)
+    m &= ~np.uint64((1 << low_zero_bits) - 1)
+    return (s | e | m).view(np.float64)
+
+
+def operand_sets(seed=7, n=400_000):
+    rng = np.random.default_rng(seed)
+    yield "whole range", rand_bits(rng, n, 1, 2046), rand_bits(rng, n, 1, 2046)
+    yield "close exponents", rand_bits(rng, n, 1000, 1050), rand_bits(rng, n, 1000, 1050)
+    a = rand_bits(rng, n, 1015, 1030)
+    near = (a.view(np.uint64) + rng.integers(-3, 4, n).astype(np.uint64)).view(np.float64)
+    yield "cancellation", a, -near
+    yield "ties", rand_bits(rng, n, 1020, 1025, 26), rand_bits(rng, n, 1020, 1025, 26)
+    yield "short b", rand_bits(rng, n, 1020, 1025), rand_bits(rng, n, 1020, 1025, 30)
+    yield "tiny", rand_bits(rng, n, 1, 130), rand_bits(rng, n, 1, 130)
+    yield "huge", rand_bits(rng, n, 1990, 2046), rand_bits(rng, n, 1, 2046)
+    ones = np.full(n, 1.0) + rng.integers(0, 1 << 20, n) * 2.0 ** -52
+    yield "carries", ones, 2.0 - ones
+    sp = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, -5e-324,
+                   2.2250738585072014e-308, -2.2250738585072014e-308,
+                   1.7976931348623157e308, -1.7976931348623157e308, 1.0, -1.0,
+                   0.5, 3.0, 2.0 ** 64, 2.0 ** -1000, -(2.0 ** -1021)])
+    A, B = np.meshgrid(sp, sp)
+    yield "special values", A.ravel(), B.ravel()
+
+
+@pytest.mark.parametrize("op", ["add", "mul"])
+def test_integer_fp64_matches_ieee(emu, op):
+    fn = emu.emu_add_n if op == "add" else emu.emu_mul_n
+    for name, a, b in operand_sets():
+        with np.errstate(all="ignore"):
+            want = a + b if op == "add" else a * b
+        assert mismatches(want, call(fn, a, b)) == 0, name
+        assert mismatches(want, call(fn, b, a)) == 0, name + " (swapped)"

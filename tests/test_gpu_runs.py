@@ -124,6 +124,25 @@ def test_resident_ppcg_matches_per_call(prec, eps, steps):
         (b[-1].vol, b[-1].mass, b[-1].ie, b[-1].temp)
 
 
+@pytest.mark.parametrize("prec,mode,inner,reflective",
+                         [("jac_block", "chain", 7, False), ("jac_block", "exact", 9, True),
+                          ("jac_diag", "fused", 5, True), ("none", "chain", 3, False),
+                          ("jac_block", "fused", 6, True)])
+def test_resident_ppcg_inner_steps(prec, mode, inner, reflective):
+    """Odd and even inner-step counts, strips cut by the top edge
+    (y_cells % 4 != 0) and reflective faces (whose operator reads the sd
+    halo) give the per-call results and the oracle's in the resident loop."""
+    deck = decks.five_state_deck(157, solver="ppcg", prec=prec, steps=3, eps=1e-13,
+                                 max_iters=2000, y_cells=143, inner_steps=inner,
+                                 presteps=12, reflective=reflective,
+                                 extra="tl_arithmetic %s" % mode)
+    res = oracle.run_deck(deck)
+    assert_matches_oracle(gpu_run(deck), res)
+    resident = gpu_run(deck, mode=lib.DRIVER_RESIDENT)
+    assert_matches_oracle(resident, res)
+    assert all(s.inner_iterations > 0 for s in resident)
+
+
 def test_reflective_check_result_deck_matches_oracle():
     deck = decks.five_state_deck(123, solver="cg", prec="jac_block", steps=3, eps=1e-12,
                                  y_cells=99, reflective=True, check_result=True,
