@@ -652,6 +652,35 @@ __global__ void __launch_bounds__(kBlock)
   });
 }
 
+// tea_leaf_ppcg_solve_calc_sd for the block-Jacobi preconditioner alone
+// (tea_leaf_ppcg_cl.cl:90-134): k_ppcg_sd's mode-1 block path with no
+// other path compiled in, so it needs fewer registers and more warps fit
+// on an SM to hide the latency of each strip's dependent sweep.
+constexpr int kSdMinBlocks = 5;
+template <int TH, int F, int MB>
+__global__ void __launch_bounds__(kBlock, MB)
+    k_ppcg_calc_sd_block(Dev d, Red red, double alpha, double beta, const ResState* st) {
+  if (st && *(volatile const int*)&st->stop) return;
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 1
+    for (int ys = y0; ys < y0 + TH && ys < d.y_max; ys += 4) {
+      double zl[4], rl[4], sv[4];
+      const long long c0 = cidx(d, x, ys);
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const bool in = ys + i < d.y_max;
+        rl[i] = in ? d.r[c0 + i * d.S] : 0.0;
+        sv[i] = in ? d.sd[c0 + i * d.S] : 0.0;
+      }
+      strip_solve<F>(d, c0, strip_rows(d, ys), rl, zl);
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+        if (ys + i < d.y_max) d.sd[c0 + i * d.S] = cheby_update<F>(alpha, sv[i], beta, zl[i]);
+    }
+  });
+}
+
 // tea_leaf_ppcg_solve_update_r, tea_leaf_ppcg_cl.cl:62-88
 template <int TH, int F>
 __global__ void __launch_bounds__(kBlock)
@@ -913,6 +942,20 @@ void launch_ppcg_update_r(Chunk& c) {
 }
 
 void launch_ppcg_calc_sd(Chunk& c, double alpha, double beta) {
+  if (c.prec == PREC_JAC_BLOCK) {
+    const Dev d4 = dev4(c);
+    const char* name = "tea_leaf_ppcg_solve_calc_sd";
+    if (c.arith == 2)
+      launch_tile_ns(c, name, d4.ns, k_ppcg_calc_sd_block<4, 2, kSdMinBlocks>, d4, c.red(),
+                     alpha, beta, (const ResState*)nullptr);
+    else if (c.arith == 1)
+      launch_tile_ns(c, name, d4.ns, k_ppcg_calc_sd_block<4, 1, kSdMinBlocks>, d4, c.red(),
+                     alpha, beta, (const ResState*)nullptr);
+    else
+      launch_tile_ns(c, name, d4.ns, k_ppcg_calc_sd_block<4, 0, kSdMinBlocks>, d4, c.red(),
+                     alpha, beta, (const ResState*)nullptr);
+    return;
+  }
   TH4_DISPATCH(c, "tea_leaf_ppcg_solve_calc_sd", k_ppcg_sd, dev4(c), c.red(), 1,
               0.0, alpha, beta, (const ResState*)nullptr);
 }
@@ -1195,7 +1238,9 @@ static void enqueue_ppcg_iterations_t(Chunk& c, int iters) {
   const int gw = tile_grid(c, k_cg_calc_w<TH, F>);
   const int gu = tile_grid(c, k_ppcg_ur_sd<TH, F>);
   const int gr = tile_grid(c, k_ppcg_update_r<4, F>, d4.ns);
-  const int gs = tile_grid(c, k_ppcg_sd<4, F>, d4.ns);
+  const bool blk = c.prec == PREC_JAC_BLOCK;
+  const int gs = blk ? tile_grid(c, k_ppcg_calc_sd_block<4, F, kSdMinBlocks>, d4.ns)
+                     : tile_grid(c, k_ppcg_sd<4, F>, d4.ns);
   const int gz = tile_grid(c, k_ppcg_rz_step<TH, F>);
   const int gp = tile_grid(c, k_cg_calc_p<4, F>, d4.ns);
   for (int i = 0; i < iters; i++) {
@@ -1203,8 +1248,12 @@ static void enqueue_ppcg_iterations_t(Chunk& c, int iters) {
     k_ppcg_ur_sd<TH, F><<<gu, kBlock, 0, c.stream>>>(d, red, st, theta);
     for (int k = 0; k < c.n_ppcg; k++) {
       k_ppcg_update_r<4, F><<<gr, kBlock, 0, c.stream>>>(d4, red, st);
-      k_ppcg_sd<4, F><<<gs, kBlock, 0, c.stream>>>(d4, red, 1, 0.0, c.ppcg_alpha_h[k],
-                                                   c.ppcg_beta_h[k], st);
+      if (blk)
+        k_ppcg_calc_sd_block<4, F, kSdMinBlocks><<<gs, kBlock, 0, c.stream>>>(
+            d4, red, c.ppcg_alpha_h[k], c.ppcg_beta_h[k], st);
+      else
+        k_ppcg_sd<4, F><<<gs, kBlock, 0, c.stream>>>(d4, red, 1, 0.0, c.ppcg_alpha_h[k],
+                                                     c.ppcg_beta_h[k], st);
     }
     k_ppcg_rz_step<TH, F><<<gz, kBlock, 0, c.stream>>>(d, red, st);
     k_cg_calc_p<4, F><<<gp, kBlock, 0, c.stream>>>(d4, red, 0.0, st, c.res_counter);
