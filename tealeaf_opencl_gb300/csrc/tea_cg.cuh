@@ -60,7 +60,7 @@ __device__ __forceinline__ void ur_values(double alpha, double& u, double p,
 template <int TH, int F, int NV, bool CG = false, bool SD = false>
 __device__ __forceinline__ void cg_ur_tile(const Dev& d, int x, int y0, bool xin,
                                            double* acc, double alpha,
-                                           double theta = 1.0) {
+                                           const DivConst& theta = DivConst{}) {
 #pragma unroll 1
   for (int g = y0; g < y0 + TH; g += 4) {
     const long long c0 = cidx(d, x, g);
@@ -101,7 +101,7 @@ __device__ __forceinline__ void cg_ur_tile(const Dev& d, int x, int y0, bool xin
       double av = 0.0, bv = 0.0;
       if (in[j]) {
         if (d.prec != PREC_NONE) d.z[c0 + j * d.S] = zv[j];
-        if (SD) d.sd[c0 + j * d.S] = (d.prec != PREC_NONE ? zv[j] : rv[j]) / theta;
+        if (SD) d.sd[c0 + j * d.S] = emu_ddiv(d.prec != PREC_NONE ? zv[j] : rv[j], theta);
         av = rv[j];
         bv = d.prec != PREC_NONE ? zv[j] : rv[j];
       }

@@ -1,4 +1,5 @@
-// Correctly rounded FP64 add and multiply on the integer pipes.
+// Correctly rounded FP64 add, multiply and division by a launch-wide
+// divisor on the integer pipes.
 //
 // GB300 issues about two FP64 lanes per clock per SM, against 128 lanes of
 // 32-bit integer and FP32 work, so every stencil kernel of the solve waits
@@ -6,10 +7,11 @@
 // functions compute IEEE 754 binary64 addition and multiplication with
 // round-to-nearest-even from the operands' bit patterns, using only integer
 // instructions, so a kernel can move part of its FP64 work off the FP64
-// pipe and still produce the hardware's results bit for bit.
+// pipe and still produce the hardware's results bit for bit.  A correctly
+// rounded FP64 division takes many FP64 instructions; emu_ddiv takes none.
 //
-// Method (textbook IEEE arithmetic, e.g. the sum and product algorithms in
-// Muller et al., Handbook of Floating-Point Arithmetic, ch. 7-8): align the
+// Method (textbook IEEE 754 arithmetic, as in Muller et al., Handbook of
+// Floating-Point Arithmetic): align the
 // significands in 64-bit integers with guard bits and a sticky bit, add or
 // multiply exactly, normalise, round to nearest even on the guard bits.
 // Operands or results outside the normal range (zeros, subnormals,
@@ -81,6 +83,70 @@ __device__ __forceinline__ double emu_dmul(double a, double b) {
   const uint64_t f = top ? hi : ((hi << 1) | (lo >> 63));
   const uint64_t below = top ? lo : (lo << 1);
   return __longlong_as_double((long long)emu_pack((ia ^ ib) & kSign, e0 + top, f, below != 0));
+}
+
+// Division by a divisor that is the same for every element of a launch
+// (the Chebyshev / PPCG theta), exactly rounded, on the integer pipes.
+// The significand quotient is an integer division by an invariant divisor:
+// Moller and Granlund, "Improved division by invariant integers" (IEEE
+// Trans. Computers 60(2), 2011), algorithm 4 (2/1 division with a
+// precomputed reciprocal), applied to the 128-bit numerator mx * 2^(65|66)
+// and the normalised divisor significand d = my * 2^11.  Its 55-bit
+// quotient and the remainder give the 53-bit significand, the round bit and
+// the sticky bit.
+struct DivConst {
+  double y;    // the divisor
+  uint64_t d;  // significand of y with its leading one at bit 63
+  uint64_t v;  // floor((2^128 - 1) / d) - 2^64
+  int ey;      // biased exponent of y
+  int ok;      // y is a normal number; otherwise the hardware divides
+};
+
+// The reciprocal constants of y (host code: 128-bit integer division).
+inline DivConst div_const(double y) {
+  DivConst k;
+  uint64_t iy;
+  static_assert(sizeof(iy) == sizeof(y), "binary64");
+  __builtin_memcpy(&iy, &y, sizeof(iy));
+  k.y = y;
+  k.ey = (int)(iy >> 52) & 0x7ff;
+  k.ok = k.ey != 0 && k.ey != 0x7ff;
+  k.d = ((iy & kFrac) | kHidden) << 11;
+  const unsigned __int128 all = ~(unsigned __int128)0;
+  k.v = (uint64_t)(all / k.d);  // the quotient is below 2^65: its low word
+  return k;
+}
+
+// x / k.y, rounded to nearest even.
+__device__ __forceinline__ double emu_ddiv(double x, const DivConst& k) {
+  const uint64_t ix = (uint64_t)__double_as_longlong(x);
+  const int ex = (int)(ix >> 52) & 0x7ff;
+  const uint64_t mx = (ix & kFrac) | kHidden;
+  const uint64_t my = k.d >> 11;
+  const int lt = mx < my ? 1 : 0;  // significand quotient below 1
+  const int e = ex - k.ey + 1023 - lt;  // biased exponent of the result
+  if (!k.ok || ex == 0 || ex == 0x7ff || e < 1 || e > 0x7fe) return x / k.y;
+  // numerator u1 * 2^64 with u1 = mx * 2^(1 + lt) < d: quotient in [2^54, 2^55)
+  const uint64_t u1 = mx << (1 + lt);
+  const uint64_t q0 = k.v * u1;
+  uint64_t q1 = __umul64hi(k.v, u1) + u1 + 1;
+  uint64_t r = 0 - q1 * k.d;
+  if (r > q0) {
+    q1 -= 1;
+    r += k.d;
+  }
+  if (r >= k.d) {
+    q1 += 1;
+    r -= k.d;
+  }
+  // q1 has 55 bits: 53 for the significand, a round bit, and one more
+  // below it that joins the remainder in the sticky bit
+  uint64_t m = q1 >> 2;
+  const bool rb = (q1 >> 1) & 1;
+  const bool sticky = (q1 & 1) || r != 0;
+  m += (rb && (sticky || (m & 1))) ? 1 : 0;
+  const uint64_t sg = (ix ^ (uint64_t)__double_as_longlong(k.y)) & kSign;
+  return __longlong_as_double((long long)(sg + ((uint64_t)(e - 1) << 52) + m));
 }
 
 }  // namespace tea

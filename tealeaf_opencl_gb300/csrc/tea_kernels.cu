@@ -487,7 +487,7 @@ __device__ __forceinline__ double cheby_update(double a, double p, double bl,
 // mode 1: p = alpha p + beta M^-1 r.
 template <int TH, int F>
 __global__ void __launch_bounds__(kBlock)
-    k_cheby_p(Dev d, Red red, int mode, double theta, double alpha,
+    k_cheby_p(Dev d, Red red, int mode, DivConst theta, double alpha,
               double beta) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
@@ -518,7 +518,7 @@ __global__ void __launch_bounds__(kBlock)
           if (ys + i < d.y_max) {
             const long long c = c0 + i * d.S;
             if (mode == 0)
-              d.p[c] = zl[i] / theta;
+              d.p[c] = emu_ddiv(zl[i], theta);
             else
               d.p[c] = cheby_update<F>(alpha, pl[i], beta, zl[i]);
           }
@@ -539,9 +539,9 @@ __global__ void __launch_bounds__(kBlock)
             rl[j] = rv;
             if (mode == 0) {
               if (d.prec == PREC_JAC_DIAG)
-                pl[j] = (d.Mi[c] * rv) / theta;
+                pl[j] = emu_ddiv(d.Mi[c] * rv, theta);
               else
-                pl[j] = rv / theta;
+                pl[j] = emu_ddiv(rv, theta);
             } else {
               if (d.prec == PREC_JAC_DIAG)
                 pl[j] = cheby_update<F>(alpha, d.p[c], beta * d.Mi[c], rv);
@@ -592,7 +592,7 @@ __global__ void __launch_bounds__(kBlock) k_cheby_calc_u(Dev d, Red red) {
 // diagonal case alpha sd + (beta r) Mi)
 template <int TH, int F>
 __global__ void __launch_bounds__(kBlock)
-    k_ppcg_sd(Dev d, Red red, int mode, double theta, double alpha,
+    k_ppcg_sd(Dev d, Red red, int mode, DivConst theta, double alpha,
               double beta, const ResState* st) {
   if (st && *(volatile const int*)&st->stop) return;
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
@@ -615,7 +615,7 @@ __global__ void __launch_bounds__(kBlock)
           if (ys + i < d.y_max) {
             const long long c = c0 + i * d.S;
             if (mode == 0)
-              d.sd[c] = zl[i] / theta;
+              d.sd[c] = emu_ddiv(zl[i], theta);
             else
               d.sd[c] = cheby_update<F>(alpha, sv[i], beta, zl[i]);
           }
@@ -633,9 +633,9 @@ __global__ void __launch_bounds__(kBlock)
             const double rv = d.r[c];
             if (mode == 0) {
               if (d.prec == PREC_JAC_DIAG)
-                nv[j] = rv * d.Mi[c] / theta;
+                nv[j] = emu_ddiv(rv * d.Mi[c], theta);
               else
-                nv[j] = rv / theta;
+                nv[j] = emu_ddiv(rv, theta);
             } else {
               if (d.prec == PREC_JAC_DIAG)
                 nv[j] = cheby_update<F>(alpha, d.sd[c], beta * rv, d.Mi[c]);
@@ -919,12 +919,12 @@ void launch_cg_calc_p(Chunk& c, double beta) {
 
 void launch_cheby_init_p(Chunk& c, double theta) {
   TH_DISPATCH(c, "tea_leaf_cheby_solve_init_p", k_cheby_p, c.dev(), c.red(), 0,
-              theta, 0.0, 0.0);
+              div_const(theta), 0.0, 0.0);
 }
 
 void launch_cheby_calc_p(Chunk& c, double alpha, double beta) {
   TH_DISPATCH(c, "tea_leaf_cheby_solve_calc_p", k_cheby_p, c.dev(), c.red(), 1,
-              0.0, alpha, beta);
+              div_const(1.0), alpha, beta);
 }
 
 void launch_cheby_calc_u(Chunk& c) {
@@ -933,7 +933,7 @@ void launch_cheby_calc_u(Chunk& c) {
 
 void launch_ppcg_init_sd(Chunk& c, double theta) {
   TH4_DISPATCH(c, "tea_leaf_ppcg_solve_init_sd", k_ppcg_sd, dev4(c), c.red(), 0,
-              theta, 0.0, 0.0, (const ResState*)nullptr);
+              div_const(theta), 0.0, 0.0, (const ResState*)nullptr);
 }
 
 void launch_ppcg_update_r(Chunk& c) {
@@ -957,7 +957,7 @@ void launch_ppcg_calc_sd(Chunk& c, double alpha, double beta) {
     return;
   }
   TH4_DISPATCH(c, "tea_leaf_ppcg_solve_calc_sd", k_ppcg_sd, dev4(c), c.red(), 1,
-              0.0, alpha, beta, (const ResState*)nullptr);
+              div_const(1.0), alpha, beta, (const ResState*)nullptr);
 }
 
 void launch_jacobi_copy_u(Chunk& c) {
@@ -1194,7 +1194,7 @@ static bool launch_cg_persistent(Chunk& c) {
 // sum is taken, and sd = M^-1 r / theta comes from the z formed here.
 template <int TH, int F>
 __global__ void __launch_bounds__(kBlock)
-    k_ppcg_ur_sd(Dev d, Red red, ResState* st, double theta) {
+    k_ppcg_ur_sd(Dev d, Red red, ResState* st, DivConst theta) {
   if (*(volatile int*)&st->stop) return;
   const double alpha = st->rro / st->pw;
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
@@ -1234,7 +1234,7 @@ static void enqueue_ppcg_iterations_t(Chunk& c, int iters) {
   const Dev d4 = dev4(c);  // the kernels that take no sum
   const Red red = c.red();
   ResState* st = c.res_state;
-  const double theta = c.ppcg_theta;
+  const DivConst theta = div_const(c.ppcg_theta);
   const int gw = tile_grid(c, k_cg_calc_w<TH, F>);
   const int gu = tile_grid(c, k_ppcg_ur_sd<TH, F>);
   const int gr = tile_grid(c, k_ppcg_update_r<4, F>, d4.ns);
@@ -1252,7 +1252,7 @@ static void enqueue_ppcg_iterations_t(Chunk& c, int iters) {
         k_ppcg_calc_sd_block<4, F, kSdMinBlocks><<<gs, kBlock, 0, c.stream>>>(
             d4, red, c.ppcg_alpha_h[k], c.ppcg_beta_h[k], st);
       else
-        k_ppcg_sd<4, F><<<gs, kBlock, 0, c.stream>>>(d4, red, 1, 0.0, c.ppcg_alpha_h[k],
+        k_ppcg_sd<4, F><<<gs, kBlock, 0, c.stream>>>(d4, red, 1, div_const(1.0), c.ppcg_alpha_h[k],
                                                      c.ppcg_beta_h[k], st);
     }
     k_ppcg_rz_step<TH, F><<<gz, kBlock, 0, c.stream>>>(d, red, st);

@@ -34,3 +34,8 @@ extern "C" void emu_add_n(const double* a, const double* b, double* o, long n) {
 extern "C" void emu_mul_n(const double* a, const double* b, double* o, long n) {
   for (long i = 0; i < n; i++) o[i] = tea::emu_dmul(a[i], b[i]);
 }
+
+extern "C" void emu_div_n(const double* a, double y, double* o, long n) {
+  const tea::DivConst k = tea::div_const(y);
+  for (long i = 0; i < n; i++) o[i] = tea::emu_ddiv(a[i], k);
+}

@@ -1,8 +1,9 @@
-"""The integer FP64 add and multiply (tea_emu.cuh) against IEEE arithmetic.
+"""The integer FP64 add, multiply and divide (tea_emu.cuh) against IEEE
+arithmetic.
 
-The stencil kernels move part of their FP64 adds and multiplies to integer
-instructions; the solve stays bit-exact only if those give the correctly
-rounded result for every operand pair.  The header is built for the host
+The stencil kernels move part of their FP64 multiplies and their divisions
+by theta to integer instructions; the solve stays bit-exact only if those
+give the correctly rounded result for every operand pair.  The header is built for the host
 here and compared bit for bit with numpy's float64 + and * on random
 operands over the whole exponent range, on the hard cases of each
 algorithm (cancellation, exact ties, carries out of the rounding) and on
@@ -82,3 +83,22 @@ def test_integer_fp64_matches_ieee(emu, op):
             want = a + b if op == "add" else a * b
         assert mismatches(want, call(fn, a, b)) == 0, name
         assert mismatches(want, call(fn, b, a)) == 0, name + " (swapped)"
+
+
+def test_integer_division_by_invariant_divisor_matches_ieee(emu):
+    emu.emu_div_n.argtypes = [P, ctypes.c_double, P, ctypes.c_long]
+    rng = np.random.default_rng(11)
+    divisors = list(rand_bits(rng, 30, 1, 2046)) + list(rand_bits(rng, 30, 1010, 1040))
+    divisors += [1.0, 3.0, 0.1, 7.0, -1.5, 1.0000000000000002, 1.9999999999999998,
+                 5e-324, 0.0, -0.0, np.inf, np.nan, 2.2250738585072014e-308,
+                 1.7976931348623157e308]
+    for y in divisors:
+        for xs in (rand_bits(rng, 40_000, 1, 2046), rand_bits(rng, 40_000, 1000, 1050),
+                   rand_bits(rng, 5_000, 1, 60), rand_bits(rng, 5_000, 1990, 2046),
+                   np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, 1.0, y, -y, 2 * y])):
+            xs = np.ascontiguousarray(xs)
+            got = np.empty_like(xs)
+            emu.emu_div_n(xs.ctypes.data_as(P), float(y), got.ctypes.data_as(P), xs.size)
+            with np.errstate(all="ignore"):
+                want = xs / y
+            assert mismatches(want, got) == 0, y
