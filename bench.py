@@ -54,6 +54,25 @@ WORKLOADS = {
 
 ARITHMETIC = "chain"  # set from --arithmetic in main()
 
+# FP64-pipe instructions per interior cell of one launch of the dominant
+# kernel, counted from its source (products done on the integer pipes are
+# not counted): update_r is r - A sd plus u + sd (chain: 5 fused
+# multiply-adds and an add; fused: 4 + 1 + 1; exact: 7 + 1 + 1); calc_ur
+# with diagonal Jacobi is u + alpha p, r - alpha w, z = Mi r, r.z (4 when
+# fused, 7 when exact) and with block Jacobi adds 2.5 for the strip sweep
+# instead of 1 for z (5.5 when fused).  These kernels are bound by GB300's
+# FP64 pipe, not by HBM.
+FP64_PER_CELL = {
+    ("tea_leaf_ppcg_solve_update_r", "jac_block", "chain"): 6,
+    ("tea_leaf_ppcg_solve_update_r", "jac_block", "fused"): 6,
+    ("tea_leaf_ppcg_solve_update_r", "jac_block", "exact"): 9,
+    ("tea_leaf_cg_solve_calc_ur", "jac_diag", "chain"): 4,
+    ("tea_leaf_cg_solve_calc_ur", "jac_diag", "fused"): 4,
+    ("tea_leaf_cg_solve_calc_ur", "jac_diag", "exact"): 7,
+    ("tea_leaf_cg_solve_calc_ur", "jac_block", "chain"): 5.5,
+    ("tea_leaf_cg_solve_calc_ur", "jac_block", "fused"): 5.5,
+}
+
 
 def deck_for(name, steps):
     from tealeaf_opencl_gb300 import decks
@@ -289,6 +308,14 @@ def run_ours(args, dist):
     achieved = (bytes_per_cell * ncell / (avg_launch_ms / 1e3) / 1e9
                 if avg_launch_ms else None)
     traffic = ncu_traffic(kernel, name)
+    fp64_n = FP64_PER_CELL.get((kernel, WORKLOADS[name][2], ARITHMETIC))
+    fp64 = None
+    if fp64_n is not None and avg_launch_ms:
+        rate = float(L.tea_gb300_fp64_rate())  # measured FP64 FMA/s, after the timed regions
+        done = fp64_n * ncell / (avg_launch_ms / 1e3)
+        fp64 = {"instructions_per_cell": fp64_n, "achieved_per_s": done,
+                "peak_per_s": rate, "peak_kind": "measured: 8 independent FMA chains per thread",
+                "frac": done / rate if rate > 0 else None}
     out = {
         "metric": "TeaLeaf %s cell-iterations/s at %dx%d (FP64)" % (WORKLOADS[name][1].upper(), cells, cells),
         "value": value,
@@ -319,7 +346,8 @@ def run_ours(args, dist):
                      "frac": achieved / peak if achieved else None,
                      "traffic": traffic,
                      "algorithmic_bytes_per_launch": bytes_per_cell * ncell,
-                     "avg_launch_ms": avg_launch_ms, "launches_timed": kn.value},
+                     "avg_launch_ms": avg_launch_ms, "launches_timed": kn.value,
+                     "fp64_pipe": fp64},
         "clocks": clk,
     }
     return out
