@@ -197,6 +197,7 @@ Red Chunk::red() const {
   rr.stride = red_stride;
   rr.counter = red_counter;
   rr.result = red_result;
+  rr.host = red_to_host ? host_map_dev : nullptr;
   return rr;
 }
 
@@ -222,6 +223,9 @@ static void free_chunk(Chunk& c) {
   c.red_counter = nullptr;
   cudaFreeHost(c.host_result);
   c.host_result = nullptr;
+  cudaFreeHost(c.host_map);
+  c.host_map = c.host_map_dev = nullptr;
+  c.red_to_host = false;
   free(c.cheby_alpha_h);
   free(c.cheby_beta_h);
   free(c.ppcg_alpha_h);
@@ -358,7 +362,11 @@ static bool init_chunk(int x_max, int y_max, const Config& cfg) {
       !check_cuda(cudaMalloc(&c.red_counter, 8 * sizeof(unsigned int)),
                   "cudaMalloc counter") ||
       !check_cuda(cudaMallocHost(&c.host_result, 8 * sizeof(double)),
-                  "cudaMallocHost"))
+                  "cudaMallocHost") ||
+      !check_cuda(cudaHostAlloc(&c.host_map, 9 * sizeof(double), cudaHostAllocMapped),
+                  "cudaHostAlloc mapped") ||
+      !check_cuda(cudaHostGetDevicePointer(&c.host_map_dev, c.host_map, 0),
+                  "cudaHostGetDevicePointer"))
     return false;
   cudaMemsetAsync(c.red_counter, 0, 8 * sizeof(unsigned int), c.stream);
   cudaMemsetAsync(c.red_result, 0, 8 * sizeof(double), c.stream);
@@ -373,10 +381,52 @@ static bool need_chunk(const char* who) {
   return true;
 }
 
-// Copies the reduced values back: every scalar-returning call is
-// synchronous, like reduceValue (ocl_reduction.hpp:6-35).
+// The next reduction launched copies its result to mapped host memory and
+// then sets the ready word there (finish_reduction), so fetch can wait on
+// that word instead of a copy and a stream synchronisation.
+static void arm_host_result(Chunk& c) {
+  __atomic_store_n((unsigned long long*)(c.host_map + 8), 0ull, __ATOMIC_RELEASE);
+  c.red_to_host = true;
+}
+
+// Returns the reduced values: every scalar-returning call is synchronous,
+// like reduceValue (ocl_reduction.hpp:6-35).  After arm_host_result the
+// host waits for the ready word (checking the stream for errors while it
+// waits, and synchronising it after a long wait); otherwise it copies the
+// result back and synchronises.
 static bool fetch(int nv, double* out) {
   Chunk& c = chunk();
+  if (c.red_to_host) {
+    c.red_to_host = false;
+    const unsigned long long* ready = (const unsigned long long*)(c.host_map + 8);
+    bool got = false;
+    for (long long spin = 0; spin < (1ll << 22); spin++) {
+      if (__atomic_load_n(ready, __ATOMIC_ACQUIRE) != 0ull) {
+        got = true;
+        break;
+      }
+      if ((spin & 1023) == 1023) {
+        const cudaError_t e = cudaStreamQuery(c.stream);
+        if (e != cudaSuccess && e != cudaErrorNotReady) {
+          check_cuda(e, "reduction wait");
+          break;
+        }
+        if (e == cudaSuccess) {  // the stream is idle: the word must be there
+          got = __atomic_load_n(ready, __ATOMIC_ACQUIRE) != 0ull;
+          break;
+        }
+      }
+    }
+    if (!got && check_cuda(cudaStreamSynchronize(c.stream), "reduction sync"))
+      got = __atomic_load_n(ready, __ATOMIC_ACQUIRE) != 0ull;
+    if (got) {
+      for (int i = 0; i < nv; i++) out[i] = ((volatile const double*)c.host_map)[i];
+      return true;
+    }
+    if (error_code() == 0) fail(27, "reduction result did not arrive");
+    for (int i = 0; i < nv; i++) out[i] = NAN;
+    return false;
+  }
   if (!check_cuda(cudaMemcpyAsync(c.host_result, c.red_result,
                                   nv * sizeof(double), cudaMemcpyDeviceToHost,
                                   c.stream),
@@ -479,6 +529,7 @@ extern "C" void field_summary_kernel_ocl_(double* vol, double* mass, double* ie,
                                           double* temp) {
   double out[4] = {NAN, NAN, NAN, NAN};
   if (need_chunk("field_summary_kernel_ocl_")) {
+    arm_host_result(chunk());
     launch_field_summary(chunk());
     fetch(4, out);
   }
@@ -554,6 +605,7 @@ extern "C" void tea_leaf_calc_2norm_kernel_ocl_(int* norm_array, double* norm) {
          *norm_array);
     return;
   }
+  arm_host_result(c);
   launch_dot(c, a, b);
   fetch(1, norm);
 }
@@ -570,6 +622,7 @@ extern "C" void tea_leaf_cg_init_kernel_ocl_(double* rro) {
     launch_block_init(c);
   else if (c.prec == PREC_JAC_DIAG)
     launch_init_jac_diag(c);
+  arm_host_result(c);
   launch_cg_init_p(c);
   fetch(1, rro);
 }
@@ -577,6 +630,7 @@ extern "C" void tea_leaf_cg_init_kernel_ocl_(double* rro) {
 extern "C" void tea_leaf_cg_calc_w_kernel_ocl_(double* pw) {
   *pw = NAN;
   if (!need_chunk("tea_leaf_cg_calc_w_kernel_ocl_")) return;
+  arm_host_result(chunk());
   launch_cg_calc_w(chunk());
   fetch(1, pw);
 }
@@ -585,6 +639,7 @@ extern "C" void tea_leaf_cg_calc_ur_kernel_ocl_(double* alpha, double* rrn) {
   const double a = *alpha;
   *rrn = NAN;
   if (!need_chunk("tea_leaf_cg_calc_ur_kernel_ocl_")) return;
+  arm_host_result(chunk());
   launch_cg_calc_ur(chunk(), a);
   fetch(1, rrn);
 }
@@ -671,6 +726,7 @@ extern "C" void tea_leaf_jacobi_solve_kernel_ocl_(double* error) {
   if (!need_chunk("tea_leaf_jacobi_solve_kernel_ocl_")) return;
   Chunk& c = chunk();
   launch_jacobi_copy_u(c);
+  arm_host_result(c);
   launch_jacobi_solve(c);
   fetch(1, error);
 }

@@ -315,7 +315,16 @@ __device__ __forceinline__ bool finish_reduction(const Red& red, int ns,
   if (!is_last) return false;
   __threadfence();
   block_final_sum<NV>(red.partials, red.stride, ns, red.result, sh);
-  if (threadIdx.x == 0) *red.counter = 0u;
+  if (threadIdx.x == 0) {
+    *red.counter = 0u;
+    if (red.host) {
+      // thread 0 wrote red.result itself (block_final_sum)
+#pragma unroll
+      for (int v = 0; v < NV; v++) red.host[v] = red.result[v];
+      __threadfence_system();
+      *(volatile unsigned long long*)(red.host + 8) = 1ull;
+    }
+  }
   return true;
 }
 
