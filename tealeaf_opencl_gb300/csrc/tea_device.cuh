@@ -146,10 +146,10 @@ __device__ __forceinline__ int strip_rows(const Dev& d, int y) {
 
 // One forward step of the strip's Thomas algorithm:
 // (r - COEF_A dp) * bfp with COEF_A = -Ky
-template <int F>
+template <int F, bool EMU = false>
 __device__ __forceinline__ double fwd(double r, double ky, double dp,
                                       double bfp) {
-  return F ? __fma_rn(ky, dp, r) * bfp : (r - (-ky) * dp) * bfp;
+  return mul_e<EMU>(F ? __fma_rn(ky, dp, r) : r - (-ky) * dp, bfp);
 }
 
 // One back-substitution step: dp - cp z
@@ -159,20 +159,21 @@ __device__ __forceinline__ double bwd(double dp, double cp, double z) {
 }
 
 // block_solve_func (tea_block_jacobi.cl:6-42) for one column of one strip:
-// z = M_block^-1 r for the strip whose first cell is at offset c0.
-template <int F>
+// z = M_block^-1 r for the strip whose first cell is at offset c0.  With
+// EMU the multiplies by bfp run on the integer pipes (same bits).
+template <int F, bool EMU = false>
 __device__ __forceinline__ void strip_solve(const Dev& d, long long c0,
                                             int upper, const double rl[4],
                                             double zl[4]) {
   const long long S = d.S;
   double dp0, dp1 = 0.0, dp2 = 0.0, dp3 = 0.0;
-  dp0 = F ? rl[0] * __ldg(d.bfp + c0) : rl[0] / __ldg(d.diag + c0);
+  dp0 = F ? mul_e<EMU>(rl[0], __ldg(d.bfp + c0)) : rl[0] / __ldg(d.diag + c0);
   if (upper > 1)
-    dp1 = fwd<F>(rl[1], __ldg(d.Ky + c0 + S), dp0, __ldg(d.bfp + c0 + S));
+    dp1 = fwd<F, EMU>(rl[1], __ldg(d.Ky + c0 + S), dp0, __ldg(d.bfp + c0 + S));
   if (upper > 2)
-    dp2 = fwd<F>(rl[2], __ldg(d.Ky + c0 + 2 * S), dp1, __ldg(d.bfp + c0 + 2 * S));
+    dp2 = fwd<F, EMU>(rl[2], __ldg(d.Ky + c0 + 2 * S), dp1, __ldg(d.bfp + c0 + 2 * S));
   if (upper > 3)
-    dp3 = fwd<F>(rl[3], __ldg(d.Ky + c0 + 3 * S), dp2, __ldg(d.bfp + c0 + 3 * S));
+    dp3 = fwd<F, EMU>(rl[3], __ldg(d.Ky + c0 + 3 * S), dp2, __ldg(d.bfp + c0 + 3 * S));
   double z0, z1 = 0.0, z2 = 0.0, z3 = 0.0;
   if (upper == 4) {
     z3 = dp3;

@@ -57,6 +57,8 @@ Dev rows4_tiling(Dev d) {
 
 static Dev dev4(const Chunk& c) { return rows4_tiling(c.dev()); }
 
+
+
 template <class... KArgs, class... Args>
 static void launch_tile_ns(Chunk& c, const char* name, int ns, void (*kernel)(KArgs...),
                            Args... args) {
@@ -318,11 +320,19 @@ __global__ void k_update_halo(Dev d, int mask, int depth) {
 
 // ---------------------------------------------------------------------------
 // interior tile kernels (TH: reduction tile height, F: fused arithmetic)
+//
+// Launch bounds are chosen per kernel by measurement at 4096^2.  Writing the
+// minimum of one block per SM explicitly changes ptxas's register budget:
+// faster for update_r (48 -> 56 registers, 192 -> 182 us), dot (67 -> 61
+// us), cheby calc_u (62.4 -> 59.5), field_summary (277 -> 267),
+// calc_residual (155 -> 153) and cg calc_p (63.3 -> 62.0); slower for
+// calc_ur (240 -> 289), cg init_p (139 -> 196), init_sd, calc_w (186 ->
+// 308) and the Chebyshev step, which keep the plain bound.
 // ---------------------------------------------------------------------------
 
 // tea_leaf_calc_residual, tea_leaf_common_cl.cl:17-36
 template <int TH, int F>
-__global__ void __launch_bounds__(kBlock) k_calc_residual(Dev d, Red red) {
+__global__ void __launch_bounds__(kBlock, 1) k_calc_residual(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
 #pragma unroll 1
@@ -344,7 +354,7 @@ __global__ void __launch_bounds__(kBlock) k_calc_residual(Dev d, Red red) {
 
 // tea_leaf_calc_2norm, tea_leaf_common_cl.cl:38-54
 template <int TH, int F>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 1)
     k_dot(Dev d, Red red, const double* a, const double* b) {
   tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
 #pragma unroll 4
@@ -455,7 +465,7 @@ __global__ void __launch_bounds__(kBlock)
 // device-resident loop it runs once per calc_ur that ran, with that
 // iteration's beta.
 template <int TH, int F>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 1)
     k_cg_calc_p(Dev d, Red red, double beta, ResState* st,
                 unsigned int* counter) {
   if (st) {
@@ -479,6 +489,44 @@ template <int F>
 __device__ __forceinline__ double cheby_update(double a, double p, double bl,
                                                double br) {
   return F ? __fma_rn(a, p, bl * br) : a * p + bl * br;
+}
+
+// tea_leaf_cheby_solve_calc_p with the block-Jacobi preconditioner alone
+// (tea_leaf_cheby_cl.cl:78-145): k_cheby_p's mode-1 block path with no
+// other path compiled in: 72 registers against 80, 340 -> 326 us at 4096^2.
+// (The integer-pipe products, in the operator or the sweep, made it slower
+// here: 352 and 388 us.)
+template <int TH, int F>
+__global__ void __launch_bounds__(kBlock, 3)
+    k_cheby_calc_p_block(Dev d, Red red, double alpha, double beta) {
+  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+#pragma unroll 1
+    for (int ys = y0; ys < y0 + TH && ys < d.y_max; ys += 4) {
+      double zl[4], rl[4] = {0.0, 0.0, 0.0, 0.0}, wl[4], pl[4];
+      const long long c0 = cidx(d, x, ys);
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        if (ys + i < d.y_max) {
+          const long long c = c0 + i * d.S;
+          wl[i] = smvp<F, false, false>(d, d.u, c);
+          rl[i] = d.u0[c] - wl[i];
+          pl[i] = d.p[c];
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        if (ys + i < d.y_max) {
+          d.w[c0 + i * d.S] = wl[i];
+          d.r[c0 + i * d.S] = rl[i];
+        }
+      }
+      strip_solve<F>(d, c0, strip_rows(d, ys), rl, zl);
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+        if (ys + i < d.y_max) d.p[c0 + i * d.S] = cheby_update<F>(alpha, pl[i], beta, zl[i]);
+    }
+  });
 }
 
 // The Chebyshev residual step shared by tea_leaf_cheby_solve_init_p and
@@ -566,7 +614,7 @@ __global__ void __launch_bounds__(kBlock)
 
 // tea_leaf_cheby_solve_calc_u, tea_leaf_cheby_cl.cl:66-76
 template <int TH, int F>
-__global__ void __launch_bounds__(kBlock) k_cheby_calc_u(Dev d, Red red) {
+__global__ void __launch_bounds__(kBlock, 1) k_cheby_calc_u(Dev d, Red red) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
 #pragma unroll 1
@@ -655,8 +703,11 @@ __global__ void __launch_bounds__(kBlock)
 // tea_leaf_ppcg_solve_calc_sd for the block-Jacobi preconditioner alone
 // (tea_leaf_ppcg_cl.cl:90-134): k_ppcg_sd's mode-1 block path with no
 // other path compiled in, so it needs fewer registers and more warps fit
-// on an SM to hide the latency of each strip's dependent sweep.
-constexpr int kSdMinBlocks = 5;
+// on an SM to hide the latency of each strip's dependent sweep.  The
+// sweep's multiplies by bfp and the product beta z run on the integer
+// pipes (tea_emu.cuh, bit-identical): 157.6 -> 145.3 us at 4096^2, and
+// 141.6 us with 6 blocks per SM (158.5 with 4).
+constexpr int kSdMinBlocks = 6;
 template <int TH, int F, int MB>
 __global__ void __launch_bounds__(kBlock, MB)
     k_ppcg_calc_sd_block(Dev d, Red red, double alpha, double beta, const ResState* st) {
@@ -673,17 +724,19 @@ __global__ void __launch_bounds__(kBlock, MB)
         rl[i] = in ? d.r[c0 + i * d.S] : 0.0;
         sv[i] = in ? d.sd[c0 + i * d.S] : 0.0;
       }
-      strip_solve<F>(d, c0, strip_rows(d, ys), rl, zl);
+      strip_solve<F, true>(d, c0, strip_rows(d, ys), rl, zl);
 #pragma unroll
       for (int i = 0; i < 4; i++)
-        if (ys + i < d.y_max) d.sd[c0 + i * d.S] = cheby_update<F>(alpha, sv[i], beta, zl[i]);
+        if (ys + i < d.y_max)
+          d.sd[c0 + i * d.S] = F ? __fma_rn(alpha, sv[i], emu_dmul(beta, zl[i]))
+                                 : alpha * sv[i] + emu_dmul(beta, zl[i]);
     }
   });
 }
 
 // tea_leaf_ppcg_solve_update_r, tea_leaf_ppcg_cl.cl:62-88
 template <int TH, int F>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 1)
     k_ppcg_update_r(Dev d, Red red, const ResState* st) {
   if (st && *(volatile const int*)&st->stop) return;
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
@@ -783,7 +836,7 @@ __global__ void __launch_bounds__(kBlock) k_finalise(Dev d, Red red) {
 // field_summary, field_summary_cl.cl:3-43 (energy argument bound to energy1,
 // ocl_kernels.cpp:466-469); the same arithmetic in both forms
 template <int TH, int F>
-__global__ void __launch_bounds__(kBlock) k_field_summary(Dev d, Red red) {
+__global__ void __launch_bounds__(kBlock, 1) k_field_summary(Dev d, Red red) {
   tile_driver<TH, 4>(d, red, [&](int x, int y0, bool xin, double* acc) {
 #pragma unroll 2
     for (int j = 0; j < TH; j++) {
@@ -923,6 +976,11 @@ void launch_cheby_init_p(Chunk& c, double theta) {
 }
 
 void launch_cheby_calc_p(Chunk& c, double alpha, double beta) {
+  if (c.prec == PREC_JAC_BLOCK) {
+    TH_DISPATCH(c, "tea_leaf_cheby_solve_calc_p", k_cheby_calc_p_block, c.dev(), c.red(),
+                alpha, beta);
+    return;
+  }
   TH_DISPATCH(c, "tea_leaf_cheby_solve_calc_p", k_cheby_p, c.dev(), c.red(), 1,
               div_const(1.0), alpha, beta);
 }
