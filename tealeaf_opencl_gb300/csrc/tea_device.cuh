@@ -167,7 +167,7 @@ __device__ __forceinline__ void strip_solve(const Dev& d, long long c0,
                                             double zl[4]) {
   const long long S = d.S;
   double dp0, dp1 = 0.0, dp2 = 0.0, dp3 = 0.0;
-  dp0 = F ? mul_e<EMU>(rl[0], __ldg(d.bfp + c0)) : rl[0] / __ldg(d.diag + c0);
+  dp0 = F ? mul_e<EMU>(rl[0], __ldg(d.bfp + c0)) : emu_ddiv_var(rl[0], __ldg(d.diag + c0));
   if (upper > 1)
     dp1 = fwd<F, EMU>(rl[1], __ldg(d.Ky + c0 + S), dp0, __ldg(d.bfp + c0 + S));
   if (upper > 2)

@@ -149,4 +149,63 @@ __device__ __forceinline__ double emu_ddiv(double x, const DivConst& k) {
   return __longlong_as_double((long long)(sg + ((uint64_t)(e - 1) << 52) + m));
 }
 
+// x / y for divisors that change from element to element, exactly rounded,
+// on the integer and FP32 pipes.  The significand quotient
+// Q = floor(mx 2^(54|55) / my) comes from a reciprocal R ~ 2^116 / my: an
+// FP32 seed (1 / the top 24 bits of my, correctly rounded) refined by two
+// fixed-point Newton steps R += R (2^116 - my R) / 2^116, then
+// Q ~ mx R / 2^(62|61).  The remainder N - Q my is then formed exactly and Q
+// corrected until 0 <= remainder < my, so the quotient is exact whatever
+// the reciprocal's error; if three corrections each way do not get there
+// (they always do: the estimate is within two of Q), the hardware divides.
+// Rounding is as in emu_ddiv.
+__device__ __forceinline__ double emu_ddiv_var(double x, double y) {
+  const uint64_t ix = (uint64_t)__double_as_longlong(x);
+  const uint64_t iy = (uint64_t)__double_as_longlong(y);
+  const int ex = (int)(ix >> 52) & 0x7ff, ey = (int)(iy >> 52) & 0x7ff;
+  const uint64_t mx = (ix & kFrac) | kHidden, my = (iy & kFrac) | kHidden;
+  const int lt = mx < my ? 1 : 0;
+  const int e = ex - ey + 1023 - lt;  // biased exponent of the result
+  if (ex == 0 || ex == 0x7ff || ey == 0 || ey == 0x7ff || e < 1 || e > 0x7fe) return x / y;
+  // seed: f ~ 2^29 / my to about 2^-22; R0 ~ 2^116 / my, below 2^64
+  const float f = __frcp_rn((float)(uint32_t)(my >> 29));
+  uint64_t R = (__float2ull_rz(f * 0x1p86f) << 1) - 1;
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    // err = 2^116 - my R as a 128-bit two's complement value; e52 = err >> 52
+    const uint64_t plo = my * R, phi = __umul64hi(my, R);
+    const uint64_t elo = 0 - plo;
+    const uint64_t ehi = (1ull << 52) - phi - (plo != 0 ? 1 : 0);
+    const long long e52 = (long long)((ehi << 12) | (elo >> 52));
+    if (e52 >= 0) {
+      const uint64_t c = __umul64hi(R, (uint64_t)e52);
+      R = c > ~R ? ~0ull : R + c;
+    } else {
+      R -= __umul64hi(R, (uint64_t)(-e52));
+    }
+  }
+  // Q ~ mx R / 2^(62 - lt), then the exact remainder N - Q my modulo 2^64
+  const uint64_t qlo = mx * R, qhi = __umul64hi(mx, R);
+  uint64_t q = (qhi << (2 + lt)) | (qlo >> (62 - lt));
+  long long rem = (long long)((mx << (54 + lt)) - q * my);
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    if (rem < 0) {
+      q -= 1;
+      rem += (long long)my;
+    }
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    if (rem >= (long long)my) {
+      q += 1;
+      rem -= (long long)my;
+    }
+  if (rem < 0 || rem >= (long long)my) return x / y;
+  uint64_t m = q >> 2;
+  const bool rb = (q >> 1) & 1;
+  const bool sticky = (q & 1) || rem != 0;
+  m += (rb && (sticky || (m & 1))) ? 1 : 0;
+  return __longlong_as_double((long long)(((ix ^ iy) & kSign) + ((uint64_t)(e - 1) << 52) + m));
+}
+
 }  // namespace tea

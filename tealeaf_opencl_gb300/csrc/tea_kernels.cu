@@ -226,13 +226,13 @@ __global__ void k_init_common(Dev d, int coef, double rx, double ry) {
     dl = d.density[c - 1];
     dd = d.density[c - d.S];
   } else if (coef == 2) {
-    dc = 1.0 / d.density[c];
-    dl = 1.0 / d.density[c - 1];
-    dd = 1.0 / d.density[c - d.S];
+    dc = emu_ddiv_var(1.0, d.density[c]);
+    dl = emu_ddiv_var(1.0, d.density[c - 1]);
+    dd = emu_ddiv_var(1.0, d.density[c - d.S]);
   }
-  double kx = (dl + dc) / (2.0 * dl * dc);
+  double kx = emu_ddiv_var(dl + dc, 2.0 * dl * dc);
   kx = kx * rx;
-  double ky = (dd + dc) / (2.0 * dd * dc);
+  double ky = emu_ddiv_var(dd + dc, 2.0 * dd * dc);
   ky = ky * ry;
   d.Kx[c] = kx;
   d.Ky[c] = ky;
@@ -270,7 +270,7 @@ __global__ void k_init_jac_diag(Dev d) {
   if (col >= d.xs || row >= d.ys) return;
   const long long c = (long long)row * d.S + col;
   const double diag = (1.0 + (d.Ky[c + d.S] + d.Ky[c]) + (d.Kx[c + 1] + d.Kx[c]));
-  d.Mi[c] = 1.0 / diag;
+  d.Mi[c] = emu_ddiv_var(1.0, diag);
 }
 
 // tea_leaf_block_init, tea_block_jacobi.cl:78-105: one thread per column of
@@ -282,14 +282,14 @@ __global__ void k_block_init(Dev d, int fused) {
   const int upper = strip_rows(d, 4 * g);
   const long long S = d.S;
   const long long c0 = cidx(d, x, 4 * g);
-  double cpv = (-d.Ky[c0 + S]) / coef_b(d, c0);
+  double cpv = emu_ddiv_var(-d.Ky[c0 + S], coef_b(d, c0));
   d.cp[c0] = cpv;
   // the fused form divides by COEF_B of the first row through its
   // reciprocal, kept in the otherwise unused bfp of that row
-  if (fused) d.bfp[c0] = 1.0 / coef_b(d, c0);
+  if (fused) d.bfp[c0] = emu_ddiv_var(1.0, coef_b(d, c0));
   for (int k = 1; k < upper; k++) {
     const long long ck = c0 + k * S;
-    const double b = 1.0 / (coef_b(d, ck) - (-d.Ky[ck]) * cpv);
+    const double b = emu_ddiv_var(1.0, coef_b(d, ck) - (-d.Ky[ck]) * cpv);
     d.bfp[ck] = b;
     cpv = (-d.Ky[ck + S]) * b;
     d.cp[ck] = cpv;
@@ -799,9 +799,9 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_solve(Dev d, Red red) {
           const double* un = d.un;
           const double kxc = d.Kx[c], kxe = d.Kx[c + 1];
           const double kyc = d.Ky[c], kyn = d.Ky[c + S];
-          const double u1 = (d.u0[c] + kxe * un[c + 1] + kxc * un[c - 1] +
-                             kyn * un[c + S] + kyc * un[c - S]) /
-                            (1.0 + (kxc + kxe) + (kyc + kyn));
+          const double u1 = emu_ddiv_var(d.u0[c] + kxe * un[c + 1] + kxc * un[c - 1] +
+                                             kyn * un[c + S] + kyc * un[c - S],
+                                         1.0 + (kxc + kxe) + (kyc + kyn));
           uv[j] = u1;
           v[j] = fabs(u1 - un[c]);
         }
@@ -825,7 +825,7 @@ __global__ void __launch_bounds__(kBlock) k_finalise(Dev d, Red red) {
       double ev[4];
 #pragma unroll
       for (int j = 0; j < 4; j++)
-        if (g + j < d.y_max) ev[j] = d.u[c0 + j * d.S] / d.density[c0 + j * d.S];
+        if (g + j < d.y_max) ev[j] = emu_ddiv_var(d.u[c0 + j * d.S], d.density[c0 + j * d.S]);
 #pragma unroll
       for (int j = 0; j < 4; j++)
         if (g + j < d.y_max) d.energy1[c0 + j * d.S] = ev[j];

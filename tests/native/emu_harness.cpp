@@ -21,6 +21,8 @@ static inline double __longlong_as_double(long long v) {
 static inline double __dadd_rn(double a, double b) { return a + b; }
 static inline double __dmul_rn(double a, double b) { return a * b; }
 static inline int __clzll(long long v) { return __builtin_clzll((unsigned long long)v); }
+static inline float __frcp_rn(float v) { return 1.0f / v; }
+static inline unsigned long long __float2ull_rz(float v) { return (unsigned long long)v; }
 static inline unsigned long long __umul64hi(unsigned long long a, unsigned long long b) {
   return (unsigned long long)(((unsigned __int128)a * b) >> 64);
 }
@@ -38,4 +40,8 @@ extern "C" void emu_mul_n(const double* a, const double* b, double* o, long n) {
 extern "C" void emu_div_n(const double* a, double y, double* o, long n) {
   const tea::DivConst k = tea::div_const(y);
   for (long i = 0; i < n; i++) o[i] = tea::emu_ddiv(a[i], k);
+}
+
+extern "C" void emu_divv_n(const double* a, const double* b, double* o, long n) {
+  for (long i = 0; i < n; i++) o[i] = tea::emu_ddiv_var(a[i], b[i]);
 }

@@ -2,7 +2,7 @@
 arithmetic.
 
 The stencil kernels move part of their FP64 multiplies and their divisions
-by theta to integer instructions; the solve stays bit-exact only if those
+to integer instructions; the solve stays bit-exact only if those
 give the correctly rounded result for every operand pair.  The header is built for the host
 here and compared bit for bit with numpy's float64 + and * on random
 operands over the whole exponent range, on the hard cases of each
@@ -102,3 +102,32 @@ def test_integer_division_by_invariant_divisor_matches_ieee(emu):
             with np.errstate(all="ignore"):
                 want = xs / y
             assert mismatches(want, got) == 0, y
+
+
+def test_integer_division_by_varying_divisor_matches_ieee(emu):
+    """emu_ddiv_var: every element its own divisor (Jacobi, init_common,
+    block_init, finalise, the exact form's strip sweep)."""
+    emu.emu_divv_n.argtypes = [P, P, P, ctypes.c_long]
+    rng = np.random.default_rng(13)
+    sets = [rand_bits(rng, 300_000, 1, 2046), rand_bits(rng, 300_000, 1000, 1050),
+            rand_bits(rng, 100_000, 1, 100), rand_bits(rng, 100_000, 1900, 2046),
+            rand_bits(rng, 100_000, 1000, 1050, 30)]
+    pairs = [(a, b) for a in sets[:2] for b in sets[:2]] + [(sets[2], sets[3]), (sets[3], sets[2]),
+                                                            (sets[4], sets[4][::-1].copy())]
+    # divisor significands at and next to the ends of the binade
+    frac = np.concatenate([np.arange(0, 2000, dtype=np.uint64),
+                           np.uint64((1 << 52) - 1) - np.arange(0, 2000, dtype=np.uint64)])
+    ys = (frac | (np.uint64(1023) << np.uint64(52))).view(np.float64)
+    for x in (1.0, 1.5, 1.9999999999999998, 1.0000000000000002, 0.1, -3.0):
+        pairs.append((np.full(ys.size, x), ys))
+    y = rand_bits(rng, 100_000, 1015, 1030)
+    near = (y.view(np.uint64) + rng.integers(-3, 4, y.size).astype(np.uint64)).view(np.float64)
+    pairs.append((near, y))
+    sp = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, 2.2250738585072014e-308,
+                   1.7976931348623157e308, 1.0, -7.5, 2.0 ** -1022, 2.0 ** 1023])
+    A, B = np.meshgrid(sp, sp)
+    pairs.append((A.ravel(), B.ravel()))
+    for a, b in pairs:
+        with np.errstate(all="ignore"):
+            want = a / b
+        assert mismatches(want, call(emu.emu_divv_n, a, b)) == 0
