@@ -1,22 +1,22 @@
-// Correctly rounded FP64 add, multiply and division by a launch-wide
-// divisor on the integer pipes.
+// Correctly rounded FP64 add, multiply and divide on the integer pipes.
 //
 // GB300 issues about two FP64 lanes per clock per SM, against 128 lanes of
 // 32-bit integer and FP32 work, so every stencil kernel of the solve waits
 // on its FP64 instructions while most issue slots stay empty.  These
-// functions compute IEEE 754 binary64 addition and multiplication with
-// round-to-nearest-even from the operands' bit patterns, using only integer
-// instructions, so a kernel can move part of its FP64 work off the FP64
-// pipe and still produce the hardware's results bit for bit.  A correctly
-// rounded FP64 division takes many FP64 instructions; emu_ddiv takes none.
+// functions compute IEEE 754 binary64 results with round-to-nearest-even
+// from the operands' bit patterns, with integer instructions (and, for the
+// division's reciprocal seed, one FP32 reciprocal), so a kernel can move
+// part of its FP64 work off the FP64 pipe and still produce the hardware's
+// results bit for bit.  A correctly rounded FP64 division takes many FP64
+// instructions; emu_ddiv and emu_ddiv_var take none.
 //
 // Method (textbook IEEE 754 arithmetic, as in Muller et al., Handbook of
-// Floating-Point Arithmetic): align the
-// significands in 64-bit integers with guard bits and a sticky bit, add or
-// multiply exactly, normalise, round to nearest even on the guard bits.
-// Operands or results outside the normal range (zeros, subnormals,
-// infinities, NaNs, overflow, underflow) take the hardware instruction
-// instead, so those cases are the hardware's by construction.
+// Floating-Point Arithmetic): align the significands in 64-bit integers with
+// guard bits and a sticky bit, add, multiply or divide exactly, normalise,
+// round to nearest even on the guard bits.  Operands or results outside the
+// normal range (zeros, subnormals, infinities, NaNs, overflow, underflow)
+// take the hardware instruction instead, so those cases are the hardware's
+// by construction.
 #pragma once
 
 #include <stdint.h>
