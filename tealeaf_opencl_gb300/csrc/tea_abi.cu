@@ -363,7 +363,8 @@ static bool init_chunk(int x_max, int y_max, const Config& cfg) {
                   "cudaMalloc counter") ||
       !check_cuda(cudaMallocHost(&c.host_result, 8 * sizeof(double)),
                   "cudaMallocHost") ||
-      !check_cuda(cudaHostAlloc(&c.host_map, 9 * sizeof(double), cudaHostAllocMapped),
+      !check_cuda(cudaHostAlloc(&c.host_map, 9 * sizeof(unsigned long long),
+                                cudaHostAllocMapped),
                   "cudaHostAlloc mapped") ||
       !check_cuda(cudaHostGetDevicePointer(&c.host_map_dev, c.host_map, 0),
                   "cudaHostGetDevicePointer"))
@@ -385,7 +386,7 @@ static bool need_chunk(const char* who) {
 // then sets the ready word there (finish_reduction), so fetch can wait on
 // that word instead of a copy and a stream synchronisation.
 static void arm_host_result(Chunk& c) {
-  __atomic_store_n((unsigned long long*)(c.host_map + 8), 0ull, __ATOMIC_RELEASE);
+  __atomic_store_n(c.host_map + 8, 0ull, __ATOMIC_RELEASE);
   c.red_to_host = true;
 }
 
@@ -398,7 +399,7 @@ static bool fetch(int nv, double* out) {
   Chunk& c = chunk();
   if (c.red_to_host) {
     c.red_to_host = false;
-    const unsigned long long* ready = (const unsigned long long*)(c.host_map + 8);
+    const unsigned long long* ready = c.host_map + 8;
     bool got = false;
     for (long long spin = 0; spin < (1ll << 22); spin++) {
       if (__atomic_load_n(ready, __ATOMIC_ACQUIRE) != 0ull) {
@@ -420,7 +421,10 @@ static bool fetch(int nv, double* out) {
     if (!got && check_cuda(cudaStreamSynchronize(c.stream), "reduction sync"))
       got = __atomic_load_n(ready, __ATOMIC_ACQUIRE) != 0ull;
     if (got) {
-      for (int i = 0; i < nv; i++) out[i] = ((volatile const double*)c.host_map)[i];
+      for (int i = 0; i < nv; i++) {
+        const unsigned long long b = __atomic_load_n(c.host_map + i, __ATOMIC_RELAXED);
+        memcpy(&out[i], &b, sizeof(double));
+      }
       return true;
     }
     if (error_code() == 0) fail(27, "reduction result did not arrive");

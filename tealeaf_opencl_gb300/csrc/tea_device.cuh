@@ -321,7 +321,8 @@ __device__ __forceinline__ bool finish_reduction(const Red& red, int ns,
     if (red.host) {
       // thread 0 wrote red.result itself (block_final_sum)
 #pragma unroll
-      for (int v = 0; v < NV; v++) red.host[v] = red.result[v];
+      for (int v = 0; v < NV; v++)
+        red.host[v] = (unsigned long long)__double_as_longlong(red.result[v]);
       __threadfence_system();
       *(volatile unsigned long long*)(red.host + 8) = 1ull;
     }

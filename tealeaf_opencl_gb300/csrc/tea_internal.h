@@ -51,9 +51,10 @@ struct Red {
   unsigned int* counter;
   double* result;       // [nvals]
   // Optional copy of the result in mapped pinned host memory for a caller
-  // waiting on the host: result values at host[0..nvals), then a nonzero
-  // word at host[8] once they are visible (see tea_abi.cu, fetch).
-  double* host = nullptr;
+  // waiting on the host: the bit patterns of the result values at
+  // host[0..nvals), then a nonzero word at host[8] once they are visible
+  // (see tea_abi.cu, fetch).
+  unsigned long long* host = nullptr;
 };
 
 // Scalar state of the device-resident CG loop: the host scalars of
@@ -100,8 +101,8 @@ struct Chunk {
   unsigned int* red_counter = nullptr;
   double* red_result = nullptr;
   double* host_result = nullptr;  // pinned, 8 doubles
-  double* host_map = nullptr;      // mapped pinned: 8 results and a ready word
-  double* host_map_dev = nullptr;  // its device address
+  unsigned long long* host_map = nullptr;      // mapped pinned: 8 results, ready word
+  unsigned long long* host_map_dev = nullptr;  // its device address
   bool red_to_host = false;        // next c.red() copies its result to host_map
   // coefficients kept on the host (passed to kernels by value) and on device
   double* cheby_alpha_h = nullptr;
