@@ -7,8 +7,10 @@
  * (gfortran trailing underscore, implicit interfaces).  Each declaration
  * cites the reference definition it replaces.  The library keeps one
  * process-global chunk, as the reference does (ocl_init.cpp:9), so there is
- * no handle.  Calls that return a scalar are synchronous; calls without an
- * output may return before the GPU finishes (one in-order CUDA stream).
+ * no handle.  Calls that return a scalar return once the kernel that forms
+ * it has written it to host memory; calls without an output may return
+ * before the GPU finishes.  All work runs on one in-order CUDA stream, so
+ * every call sees the effects of the calls before it.
  *
  * Errors: by default a fatal error prints a message and aborts the process,
  * like cloverDie (ocl_errors.cpp:175-194).  tea_gb300_set_abort_on_error(0)
