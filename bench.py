@@ -21,7 +21,8 @@ e2e   : the same metric through the per-call C ABI (two host round trips
         pinned memory and the result field (energy1) copied back inside the
         timed region.
 --impl reference times the CPU restatement of the reference (oracle/) on
-the host cores on bounded samples of the same workload; see the design doc.
+the host cores, all threads, on bounded samples of the same workload: each
+step is one timestep capped at --cpu-cap outer iterations.
 
 Multi-GPU (torchrun): every rank solves its own copy of the problem
 (replicas; the solve is not sharded), value = all ranks' cell-iterations /
