@@ -153,7 +153,8 @@ __device__ __forceinline__ double emu_ddiv(double x, const DivConst& k) {
 // on the integer and FP32 pipes.  The significand quotient
 // Q = floor(mx 2^(54|55) / my) comes from a reciprocal R ~ 2^116 / my: an
 // FP32 seed (1 / the top 24 bits of my, correctly rounded) refined by two
-// fixed-point Newton steps R += R (2^116 - my R) / 2^116, then
+// fixed-point Newton-Raphson steps for the reciprocal,
+// R += R (2^116 - my R) / 2^116, each doubling the correct bits, then
 // Q ~ mx R / 2^(62|61).  The remainder N - Q my is then formed exactly and Q
 // corrected until 0 <= remainder < my, so the quotient is exact whatever
 // the reciprocal's error; if three corrections each way do not get there
