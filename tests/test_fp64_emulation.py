@@ -131,3 +131,23 @@ def test_integer_division_by_varying_divisor_matches_ieee(emu):
         with np.errstate(all="ignore"):
             want = a / b
         assert mismatches(want, call(emu.emu_divv_n, a, b)) == 0
+
+
+def test_integer_fp64_long_random_sweep(emu):
+    """Ten million random operand pairs per operation, exponents near 1 and
+    over the whole range, against numpy."""
+    emu.emu_divv_n.argtypes = [P, P, P, ctypes.c_long]
+    emu.emu_div_n.argtypes = [P, ctypes.c_double, P, ctypes.c_long]
+    rng = np.random.default_rng(2024)
+    for _ in range(5):
+        for elo, ehi in ((1000, 1050), (1, 2046)):
+            a = rand_bits(rng, 1_000_000, elo, ehi)
+            b = rand_bits(rng, 1_000_000, elo, ehi)
+            with np.errstate(all="ignore"):
+                assert mismatches(a + b, call(emu.emu_add_n, a, b)) == 0
+                assert mismatches(a * b, call(emu.emu_mul_n, a, b)) == 0
+                assert mismatches(a / b, call(emu.emu_divv_n, a, b)) == 0
+                y = float(b[0])
+                got = np.empty_like(a)
+                emu.emu_div_n(a.ctypes.data_as(P), y, got.ctypes.data_as(P), a.size)
+                assert mismatches(a / y, got) == 0
