@@ -20,9 +20,17 @@ e2e   : the same metric through the per-call C ABI (two host round trips
         step's input fields (density, energy1) copied host->device from
         pinned memory and the result field (energy1) copied back inside the
         timed region.
+mixed : FP64 CG and FP32-inner / FP64-refined CG to the same 1e-10
+        relative FP64 residual at 4096^2 (diagonal Jacobi), 3 timesteps:
+        their wall times and ratio, final recomputed residuals and the
+        field_summary difference (--no-mixed leaves it out).
 --impl reference times the CPU restatement of the reference (oracle/) on
-the host cores, all threads, on bounded samples of the same workload: each
-step is one timestep capped at --cpu-cap outer iterations.
+the host cores, all threads, on bounded samples of the same workload: the
+first (warm-up) step runs its CG iterations to the switch and the
+eigenvalue estimate, and every PPCG or Chebyshev step ends
+--cpu-cap-after-switch iterations after its switch, so the timed steps
+are PPCG outer iterations with their inner steps, as on the GPU (CG
+workloads: each step capped at --cpu-cap iterations).
 
 Multi-GPU (torchrun): every rank solves its own copy of the problem
 (replicas; the solve is not sharded), value = all ranks' cell-iterations /
@@ -458,31 +466,58 @@ def lognormal_factor(n, sigma=0.5, corr=8.0, seed=2024):
 def run_mixed(args):
     """FP64 CG and FP32-inner/FP64-refined CG to the same true relative
     FP64 residual (1e-10), on the same problem; wall time per timestep."""
+    return mixed_compare(args.cells, args.steps, args.lognormal, args.mixed_solver,
+                         args.inner_steps, args.presteps)
+
+
+MIXED_DEFAULT_STEPS = 3
+
+
+def mixed_summary(args):
+    """The mixed-precision comparison on the default line: 4096^2, the
+    five-state problem, CG + diagonal Jacobi, both solves to a 1e-10
+    relative FP64 residual, MIXED_DEFAULT_STEPS timesteps (the full
+    precision configuration is --mode mixed --cells 8192 --lognormal
+    --steps 10)."""
+    r = mixed_compare(4096, MIXED_DEFAULT_STEPS, False, "cg", 10, 25)
+    return {"cells": r["cells"], "steps": r["steps"], "tol": r["tol"],
+            "solver": "CG + jac_diag; mixed: FP32 inner CG in FP64 defect correction",
+            "fp64_seconds": r["fp64"]["seconds"], "mixed_seconds": r["mixed"]["seconds"],
+            "time_ratio_mixed_over_fp64": r["time_ratio_mixed_over_fp64"],
+            "fp64_final_relative_residual": r["fp64"]["relative_residual"],
+            "mixed_final_relative_residual": r["mixed"]["relative_residual"],
+            "field_summary_rel_diff": r["field_summary_rel_diff"],
+            "fp64_iterations": r["fp64"]["iterations"],
+            "mixed_fp32_iterations": r["mixed"]["iterations"],
+            "mixed_corrections": r["mixed"]["corrections"],
+            "fp64_arithmetic": r["fp64_arithmetic"],
+            "timing": "wall time per timestep, CUDA-synchronised, summed"}
+
+
+def mixed_compare(cells, steps, lognormal, mixed_solver, inner_steps, presteps):
     from tealeaf_opencl_gb300 import decks, lib
     L = lib.load()
-    cells = args.cells
-    factor = lognormal_factor(cells) if args.lognormal else None
-    out = {"mode": "mixed", "cells": cells * cells, "steps": args.steps,
-           "lognormal": bool(args.lognormal), "tol": 1e-10}
-    ncell = cells * cells
-    out["mixed_inner_solver"] = args.mixed_solver
+    factor = lognormal_factor(cells) if lognormal else None
+    out = {"mode": "mixed", "cells": cells * cells, "steps": steps,
+           "lognormal": bool(lognormal), "tol": 1e-10}
+    out["mixed_inner_solver"] = mixed_solver
     out["fp64_arithmetic"] = ARITHMETIC
     for name, extra, mode in (("fp64", "tl_exit_true_residual\ntl_arithmetic %s" % ARITHMETIC,
                                lib.DRIVER_RESIDENT),
                               ("mixed", "tl_mixed_precision\ntl_mixed_inner_eps 1e-5\n"
                                "tl_arithmetic %s" % ARITHMETIC, lib.DRIVER_PER_CALL)):
-        solver = args.mixed_solver if name == "mixed" else "cg"
+        solver = mixed_solver if name == "mixed" else "cg"
         deck = decks.five_state_deck(cells, solver=solver, prec="jac_diag",
-                                     steps=args.steps, eps=1e-10, max_iters=100000,
+                                     steps=steps, eps=1e-10, max_iters=100000,
                                      summary_frequency=0, check_result=True, extra=extra,
-                                     inner_steps=args.inner_steps if solver == "ppcg" else None,
-                                     presteps=args.presteps if solver == "ppcg" else None)
+                                     inner_steps=inner_steps if solver == "ppcg" else None,
+                                     presteps=presteps if solver == "ppcg" else None)
         drv = lib.Driver(deck, mode=mode)
         if factor is not None:
             lib.write_field("density", lib.read_field("density") * factor)
         L.tea_gb300_synchronize()
         times, infos = [], []
-        for _ in range(args.steps):
+        for _ in range(steps):
             t0 = time.perf_counter()
             infos.append(drv.step())
             L.tea_gb300_synchronize()
@@ -675,37 +710,54 @@ def run_adjoint(args):
     return out
 
 
-def cpu_sample(name, steps_timed, cap):
-    """Oracle on the same deck: one warm-up step, then steps_timed steps,
-    every step capped at `cap` outer iterations; returns (value, detail)."""
+def oracle_sample(name, steps, first_timed, cap, cap_after_switch):
+    """The oracle on the workload's deck for `steps` timesteps, bounded:
+    CG workloads cap every step at `cap` outer iterations; Chebyshev and
+    PPCG steps end `cap_after_switch` iterations after their switch from CG,
+    so the first step runs its CG iterations to the switch and the
+    eigenvalue estimate (as on the GPU), and every later PPCG step is one CG
+    iteration and then PPCG outer iterations with their inner steps.  Steps
+    first_timed.. are measured.  Returns (value, description, threads)."""
     from oracle import oracle
     cells = WORKLOADS[name][0]
-    deck = deck_for(name, 1 + steps_timed)
-    res = oracle.run_deck(deck, max_solver_iters=cap)
-    its = sum(res.iterations[1:1 + steps_timed]) + sum(res.inner_iterations[1:1 + steps_timed])
-    secs = sum(res.step_seconds[1:1 + steps_timed])
-    return its * cells * cells / secs, {
-        "iterations": its, "seconds": secs,
-        "threads": oracle.lib().oracle_num_threads()}
+    solver = WORKLOADS[name][1]
+    deck = deck_for(name, steps)
+    if solver == "cg":
+        res = oracle.run_deck(deck, max_solver_iters=cap)
+        bound = "each step capped at %d CG iterations" % cap
+    else:
+        res = oracle.run_deck(deck, max_after_switch=cap_after_switch)
+        bound = ("each step ended %d iterations after its switch from CG (step 1 "
+                 "switched after %d CG iterations)" % (cap_after_switch,
+                                                      res.switch_iteration[0] - 1))
+    sl = slice(first_timed, steps)
+    outer, inner = sum(res.iterations[sl]), sum(res.inner_iterations[sl])
+    cg = sum(max(0, s - 1) if s else it for s, it in
+             zip(res.switch_iteration[sl], res.iterations[sl]))
+    secs = sum(res.step_seconds[sl])
+    value = (outer + inner) * cells * cells / secs
+    desc = ("oracle (C/OpenMP restatement of the reference) on the same deck, "
+            "timesteps %d-%d timed of %d, %s: %d outer iterations (%d CG, %d %s) "
+            "+ %d PPCG inner steps, %.1f s"
+            % (first_timed + 1, steps, steps, bound, outer, cg, outer - cg,
+               solver.upper(), inner, secs))
+    return value, desc, oracle.lib().oracle_num_threads(), secs
+
+
+def cpu_sample(name, args):
+    """Our arm's cpu_baseline: the oracle, step 2 of a two-step run."""
+    return oracle_sample(name, 2, 1, args.cpu_cap, args.cpu_cap_after_switch)[:3]
 
 
 def run_reference(args, dist):
     """The CPU restatement of the reference on the host cores."""
-    from oracle import oracle
     name = args.workload
     cells = WORKLOADS[name][0]
-    cap = args.cpu_cap
-    deck = deck_for(name, args.warmup + args.steps)
-    t0 = time.perf_counter()
-    res = oracle.run_deck(deck, max_solver_iters=cap)
-    wall = time.perf_counter() - t0
     w, k = args.warmup, args.steps
-    its = sum(res.iterations[w:w + k]) + sum(res.inner_iterations[w:w + k])
-    secs = sum(res.step_seconds[w:w + k])
-    value = its * cells * cells / secs
-    threads = oracle.lib().oracle_num_threads()
-    sample = ("%d timesteps after %d warm-up steps, each capped at %d outer "
-              "iterations (%d iterations, %.1f s)" % (k, w, cap, its, secs))
+    t0 = time.perf_counter()
+    value, sample, threads, secs = oracle_sample(name, w + k, w, args.cpu_cap,
+                                                 args.cpu_cap_after_switch)
+    wall = time.perf_counter() - t0
     return {
         "impl": "reference",
         "metric": "TeaLeaf %s cell-iterations/s at %dx%d (FP64)" % (WORKLOADS[name][1].upper(), cells, cells),
@@ -730,8 +782,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ppcg4096", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-cap", type=int, default=24,
-                    help="outer iterations per CPU sample step (must exceed the "
-                         "CG steps before the switch for PPCG/Chebyshev)")
+                    help="CG workloads: outer iterations per CPU sample step")
+    ap.add_argument("--cpu-cap-after-switch", type=int, default=9,
+                    help="PPCG/Chebyshev workloads: iterations per CPU sample step "
+                         "from the switch from CG on")
+    ap.add_argument("--no-mixed", action="store_true",
+                    help="leave out the mixed-precision comparison of the default line")
     ap.add_argument("--cap", type=int, default=0,
                     help="limit solver iterations per GPU step (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -794,15 +850,12 @@ def main():
 
     dist = Dist()
     out = run_ours(args, dist)
+    if dist.world == 1 and not args.no_mixed:
+        out["mixed"] = mixed_summary(args)
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        value, detail = cpu_sample(args.workload, 1, args.cpu_cap)
-        out["cpu_baseline"] = {
-            "value": value, "unit": "cell-iters/s", "cores": detail["threads"],
-            "kind": "port",
-            "sample": "oracle (C/OpenMP restatement of the reference) on the same "
-                      "deck: step 2 after one warm-up step, capped at %d outer "
-                      "iterations (%d iterations, %.1f s)"
-                      % (args.cpu_cap, detail["iterations"], detail["seconds"])}
+        value, sample, threads = cpu_sample(args.workload, args)
+        out["cpu_baseline"] = {"value": value, "unit": "cell-iters/s", "cores": threads,
+                               "kind": "port", "sample": sample}
     if dist.rank == 0:
         print(json.dumps(out))
     dist.close()

@@ -217,12 +217,20 @@ int tea_gb300_set_arithmetic(int form);
  * Returns 0, or -1 for another value. */
 int tea_gb300_set_resident_mode(int mode);
 int tea_gb300_get_arithmetic(void);
+/* The persistent loop's grid barrier (mode 2 above): a block polls at most
+ * spin_limit times (default 2^26, about 4 s) before it gives up, sets the
+ * loop's error flag and returns; the call then fails with error 25.
+ * extra_arrivals = 1 makes the barrier wait for one block more than the
+ * grid has, so the wait always runs out: the test of that path uses it with
+ * a short limit.  Use 2^26 and 0 for normal runs.  Returns 0 or -1. */
+int tea_gb300_set_barrier_limits(long long spin_limit, int extra_arrivals);
 
 /* 1 (default): fatal errors abort; 0: record and return. */
 void tea_gb300_set_abort_on_error(int abort_on_error);
 
-/* 0 if no error was recorded since the last call, else the error code; the
- * message is copied to msg (may be NULL).  Clears the recorded error. */
+/* 0 if no error was recorded since the last call, else the code of the most
+ * recent error; its message is copied to msg (may be NULL).  Clears the
+ * recorded error. */
 int tea_gb300_last_error(char* msg, int msg_len);
 
 /* Frees the chunk's device memory. */
@@ -270,6 +278,25 @@ int tea_gb300_kernel_timer_read_name(const char* name, double* total_ms,
  * current GPU (independent chains, all SMs).  Needs an initialised chunk. */
 double tea_gb300_fp64_rate(void);
 
+/* No counterpart in the reference; a check of this library's own
+ * arithmetic.  The solver kernels compute some FP64 multiplies and
+ * divisions from the operands' bit patterns with integer instructions,
+ * correctly rounded.  This runs that device code on n operand pairs
+ * (device pointers a, b) beside the GPU's own FP64 instruction and counts
+ * the results whose bits differ (NaN counts as equal to NaN):
+ *   TEA_EMU_MUL            a*b     against __dmul_rn
+ *   TEA_EMU_DIV_INVARIANT  a/divisor, one divisor for all (b unused)
+ *   TEA_EMU_DIV            a/b     against __ddiv_rn
+ *   TEA_EMU_ADD            a+b     against __dadd_rn
+ * *first_mismatch is the lowest index that differs, or -1.  Synchronous;
+ * allocates two words of device memory.  Returns 0 or -1. */
+#define TEA_EMU_MUL 0
+#define TEA_EMU_DIV_INVARIANT 1
+#define TEA_EMU_DIV 2
+#define TEA_EMU_ADD 3
+int tea_gb300_emu_check(int op, const double* a, const double* b, long long n,
+                        double divisor, long long* mismatches, long long* first_mismatch);
+
 /* No counterpart in the reference.  The dot product sum(a*b) over the
  * interior of two padded FP64 fields, for callers that cannot allocate GPU
  * memory (their device memory is held by another allocator, or they must
@@ -277,17 +304,22 @@ double tea_gb300_fp64_rate(void);
  * the inputs and to one double for the result; nothing is allocated.  The
  * reduction's scratch is a fixed device array inside this library (512 KiB,
  * held on every GPU that loads the library until the process exits), which
- * limits the interior to at most 65536 partial sums (16384 x 16384 cells);
- * larger sizes are rejected with an error.  Layout: element (col,row) at
+ * holds 65536 partial sums, one per supertile of the fixed summation order:
+ * ceil(ceil(x_max/32)/8) * ceil(y_max/TH) <= 65536, TH being
+ * tea_gb300_reduction_rows(x_max, y_max).  16384 x 16384 cells fit; larger
+ * interiors are rejected with an error.  Layout: element (col,row) at
  * a[row*stride + col], interior at [halo, halo+x_max) x [halo, halo+y_max).
- * Summation order and arithmetic form are those of
- * tea_leaf_calc_2norm_kernel_ocl_, so equal inputs give equal bits.
- * Queued on `stream` (a cudaStream_t; NULL for the default stream) and
- * returns before the GPU finishes.  The first call on a device looks up
+ * The summation order is that of tea_leaf_calc_2norm_kernel_ocl_, and the
+ * arithmetic form follows tea_gb300_set_arithmetic (default fused; the
+ * chain form sums as fused does): equal inputs and equal forms give equal
+ * bits.  Queued on `stream` (a cudaStream_t; NULL for the default stream)
+ * and returns before the GPU finishes.  The first call on a device looks up
  * the scratch's device address; make that first call before any stream
- * capture.  All calls share the scratch: calls that can overlap on the GPU
- * (different streams, no ordering between them) race and give wrong
- * results.  Returns 0, or -1 (see tea_gb300_last_error). */
+ * capture, from one host thread.  All calls share the scratch: calls that
+ * can overlap on the GPU (different streams, no ordering between them) race
+ * and give wrong results.  Returns 0; an error aborts the process in the
+ * library's default mode, and returns -1 (see tea_gb300_last_error) only
+ * after tea_gb300_set_abort_on_error(0). */
 int tea_gb300_dot_noalloc(const double* a, const double* b, int x_max,
                           int y_max, int halo, long long stride,
                           double* result, void* stream);
@@ -352,6 +384,8 @@ typedef struct {
   double qa_diff;
   int outer_corrections;  /* mixed precision: FP64 corrections (else 0) */
   double relative_residual; /* mixed precision: final ||r||/||r0|| (FP64) */
+  int switch_iteration;   /* iteration of the switch from CG to Chebyshev or
+                             PPCG in this step (0: none) */
 } tea_gb300_step_info;
 
 /* Parses a tea.in deck (its text), sets up the problem on the GPU (as
@@ -365,6 +399,20 @@ int tea_gb300_driver_open(const char* deck_text, const char* log_path,
 int tea_gb300_driver_step(tea_gb300_step_info* info);
 /* Closes the log; the chunk stays allocated for inspection. */
 void tea_gb300_driver_close(void);
+
+/* Checks the reference does not make (it runs on silently,
+ * tea_solve.f90:270-330), off by default:
+ *   TEA_CHECK_BREAKDOWN  p.w <= 0 or not finite (error 70), a non-finite
+ *                        r.z, r.r or Jacobi error (71): the step fails;
+ *   TEA_CHECK_MAX_ITERS  a step that used all tl_max_iters iterations
+ *                        without meeting tl_eps fails (72). */
+#define TEA_CHECK_BREAKDOWN 1
+#define TEA_CHECK_MAX_ITERS 2
+/* For the open driver: checks (TEA_CHECK_* flags), and cap_after_switch > 0
+ * to end every Chebyshev or PPCG step that many iterations after its switch
+ * from CG (the switch's own iteration counted; 0: no such limit), so that a
+ * bounded sample still reaches the polynomial solver.  Returns 0 or -1. */
+int tea_gb300_driver_set_limits(int cap_after_switch, int checks);
 
 /* ---- batched solves (no counterpart in the reference) ----
  *

@@ -37,6 +37,7 @@ class OracleResult(C.Structure):
         ("qa_diff", C.c_double),
         ("outer_corrections", C.c_int * 1024),
         ("relative_residual", C.c_double * 1024),
+        ("switch_iteration", C.c_int * 1024),
     ]
 
     def summaries(self):
@@ -94,7 +95,7 @@ def lib():
             "oracle_set_arithmetic": (None, [i]),
             "oracle_get_arithmetic": (i, []),
             "oracle_reduction_rows": (i, [i, i]),
-            "oracle_run_deck": (i, [C.c_char_p, C.c_char_p, i,
+            "oracle_run_deck": (i, [C.c_char_p, C.c_char_p, i, i,
                                     C.POINTER(OracleResult), C.c_char_p, i]),
             "oracle_num_threads": (i, []),
             "oracle_mixed_solve": (i, [d, d, i, i, C.POINTER(MixedInfo)]),
@@ -112,13 +113,17 @@ def _pd(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
-def run_deck(deck_text, log_path=None, max_solver_iters=0):
-    """Run a tea.in deck on the oracle; returns an OracleResult."""
+def run_deck(deck_text, log_path=None, max_solver_iters=0, max_after_switch=0):
+    """Run a tea.in deck on the oracle; returns an OracleResult.
+    max_solver_iters > 0 caps every step's solver iterations;
+    max_after_switch > 0 ends each Chebyshev/PPCG step that many iterations
+    after its switch from CG (the switch's own iteration counted)."""
     res = OracleResult()
     err = C.create_string_buffer(512)
     rc = lib().oracle_run_deck(deck_text.encode(),
                                log_path.encode() if log_path else None,
-                               int(max_solver_iters), C.byref(res), err, 512)
+                               int(max_solver_iters), int(max_after_switch),
+                               C.byref(res), err, 512)
     if rc != 0:
         raise RuntimeError("oracle run failed: " + err.value.decode())
     return res

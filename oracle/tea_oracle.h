@@ -157,14 +157,18 @@ typedef struct {
   double qa_diff;
   int outer_corrections[1024]; /* mixed precision: FP64 corrections */
   double relative_residual[1024];
+  int switch_iteration[1024]; /* iteration of the switch to Chebyshev/PPCG, 0 if none */
 } oracle_result;
 
 /* Parse tea.in text and run it.  log_path may be NULL; otherwise a tea.out
  * style log is written there.  max_solver_iters > 0 caps tl_max_iters (for
- * bounded timing samples).  Returns 0 on success. */
+ * bounded timing samples).  max_after_switch > 0 ends a Chebyshev or PPCG
+ * step after that many iterations from the switch on (the iteration of the
+ * switch included), so a bounded sample still reaches the switch and then
+ * runs the polynomial solver.  Returns 0 on success. */
 int oracle_run_deck(const char* deck_text, const char* log_path,
-                    int max_solver_iters, oracle_result* result,
-                    char* err, int errlen);
+                    int max_solver_iters, int max_after_switch,
+                    oracle_result* result, char* err, int errlen);
 
 int oracle_num_threads(void);
 

@@ -470,6 +470,7 @@ typedef struct {
   double dt;
   int complete;
   int max_iters_cap;
+  int max_after_switch; /* > 0: outer iterations allowed after the switch */
 } Run;
 
 static double now_s(void) {
@@ -555,7 +556,8 @@ static int tea_leaf(Run* R, int step_index) {
   const int use_ppcg = D->solver == ORC_SOLVER_PPCG;
   const int use_jacobi = D->solver == ORC_SOLVER_JACOBI;
   const int cap = R->max_iters_cap > 0 ? R->max_iters_cap : max_iters;
-  const int loop_max = cap < max_iters ? cap : max_iters;
+  int loop_max = cap < max_iters ? cap : max_iters;
+  int switch_n = 0;
 
   double *cg_alphas = (double*)calloc((size_t)max_iters + 1, sizeof(double));
   double *cg_betas = (double*)calloc((size_t)max_iters + 1, sizeof(double));
@@ -651,6 +653,10 @@ static int tea_leaf(Run* R, int step_index) {
                         D->ppcg_inner_steps);
         }
         R->cn = R->eigmax / R->eigmin;
+        switch_n = n;
+        /* a bounded sample: this and max_after_switch - 1 more iterations */
+        if (R->max_after_switch > 0 && n - 1 + R->max_after_switch < loop_max)
+          loop_max = n - 1 + R->max_after_switch;
         logf_(R, "Switching after %3d CG its, error %15.7E\n", n, rro);
         logf_(R, "Eigen min%14.6E Eigen max%14.6E Condition number%14.6f Error%14.6E\n",
               R->eigmin, R->eigmax, R->cn, old_error);
@@ -741,6 +747,7 @@ static int tea_leaf(Run* R, int step_index) {
   if (step_index < 1024) {
     res->iterations[step_index] = performed;
     res->inner_iterations[step_index] = ppcg_inner_iters;
+    res->switch_iteration[step_index] = switch_n;
     res->conduction_error[step_index] = error / initial_residual;
     res->exact_error[step_index] =
         D->tl_check_result ? exact_error / initial_residual : NAN;
@@ -756,8 +763,8 @@ static int tea_leaf(Run* R, int step_index) {
 }
 
 int oracle_run_deck(const char* deck_text, const char* log_path,
-                    int max_solver_iters, oracle_result* result, char* err,
-                    int errlen) {
+                    int max_solver_iters, int max_after_switch,
+                    oracle_result* result, char* err, int errlen) {
   Deck* D = (Deck*)malloc(sizeof(Deck));
   if (parse_deck(deck_text, D, err, errlen) != 0) {
     free(D);
@@ -771,6 +778,7 @@ int oracle_run_deck(const char* deck_text, const char* log_path,
   R.R = result;
   R.first = 1;
   R.max_iters_cap = max_solver_iters;
+  R.max_after_switch = max_after_switch;
   if (log_path) R.log = fopen(log_path, "w");
 
   oracle_set_arithmetic(D->fused);

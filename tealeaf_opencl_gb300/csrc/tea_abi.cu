@@ -41,10 +41,8 @@ void fail(int code, const char* fmt, ...) {
   vsnprintf(buf, sizeof(buf), fmt, ap);
   va_end(ap);
   g_err_count++;
-  if (g_err_code == 0) {
-    g_err_code = code;
-    g_err_msg = buf;
-  }
+  g_err_code = code;  // the most recent error is the one reported
+  g_err_msg = buf;
   fprintf(stderr, "@@@@@\nFatal error in libtealeaf_gb300: %s\n", buf);
   if (g_abort_on_error) {
     fprintf(stderr, "Exiting\n");
@@ -743,13 +741,16 @@ extern "C" void tea_leaf_common_finalise_kernel_ocl_(void) {
 extern "C" void print_opencl_profiling_info_(void) {
   Chunk& c = chunk();
   if (!c.profiler_on) return;
+  // one row per kernel name, in name order, in the reference's layout
+  // (ocl_errors.cpp:207-228)
   fprintf(stdout, "@@@@@ CUDA Profiling information @@@@@\n");
   for (auto& kv : g_prof) {
     if (kv.second.calls)
-      fprintf(stdout, "%30s : %10.3f ms (%.2f us avg. over %lld calls)\n",
+      fprintf(stdout, "%30s : %10.3f ms (%.2f \xce\xbcs avg. over %lld calls)\n",
               kv.first.c_str(), kv.second.ms,
               1e3 * kv.second.ms / (double)kv.second.calls, kv.second.calls);
   }
+  fflush(stdout);
 }
 
 static void pack_unpack(int* fields, const char* who) {
@@ -817,6 +818,17 @@ extern "C" int tea_gb300_set_resident_mode(int mode) {
   }
   g_config.resident_mode = mode;
   chunk().resident_mode = mode;
+  return 0;
+}
+
+extern "C" int tea_gb300_set_barrier_limits(long long spin_limit, int extra_arrivals) {
+  if (spin_limit < 1 || extra_arrivals < 0 || extra_arrivals > 1) {
+    fail(3, "tea_gb300_set_barrier_limits: spin limit %lld, extra arrivals %d", spin_limit,
+         extra_arrivals);
+    return -1;
+  }
+  chunk().barrier_spin_limit = spin_limit;
+  chunk().barrier_extra = extra_arrivals;
   return 0;
 }
 

@@ -146,6 +146,18 @@ __device__ __forceinline__ void cg_scalar_step(ResState* st, double alpha,
                                                const double* result) {
   const double rrn = result[0];
   const int n = st->n;
+  if (st->check) {
+    // breakdown (the caller asked for the check; the reference runs on)
+    const double pw = st->pw;
+    const int b = !(pw > 0.0) || isinf(pw) ? 1 : (isfinite(rrn) ? 0 : 2);
+    if (b) {
+      st->breakdown = b;
+      st->breakdown_n = n;
+      st->stop = 1;
+      st->p_pending = 0;
+      return;
+    }
+  }
   const double beta = rrn / st->rro;
   if (st->alphas) {
     st->alphas[n] = alpha;

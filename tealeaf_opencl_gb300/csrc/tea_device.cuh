@@ -267,10 +267,16 @@ __device__ __forceinline__ double block_final_value(const double* partials, int 
 // Barrier across every block of a cooperative launch (all blocks resident).
 // bar[0] counts arrivals, bar[1] is the generation.  Every thread's earlier
 // global writes are visible to every block after it.  A block waits at most
-// kBarrierSpins polls (about 4 s); on time-out, or when another block has
-// timed out, it sets *err and returns false, and the kernel must return.
+// spin_limit polls (kBarrierSpins, about 4 s, unless the caller sets
+// another); on time-out, or when another block has timed out, it sets *err
+// and returns false, and the kernel must return.  The barrier opens when
+// gridDim.x + extra blocks have arrived: extra is 0, except in the test that
+// makes the wait run out (one arrival more than the grid has, so no block
+// opens it).
 constexpr long long kBarrierSpins = 1LL << 26;
-__device__ __forceinline__ bool grid_barrier(unsigned int* bar, int* err) {
+__device__ __forceinline__ bool grid_barrier(unsigned int* bar, int* err,
+                                             long long spin_limit = kBarrierSpins,
+                                             unsigned int extra = 0) {
   __shared__ int ok;
   __threadfence();
   __syncthreads();
@@ -279,14 +285,14 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* bar, int* err) {
     volatile unsigned int* gen = bar + 1;
     const unsigned int g = *gen;
     __threadfence();
-    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+    if (atomicAdd(bar, 1u) == gridDim.x - 1 + extra) {
       atomicExch(bar, 0u);
       __threadfence();
       atomicAdd(bar + 1, 1u);
     } else {
       long long spins = 0;
       while (*gen == g) {
-        if (++spins > kBarrierSpins || *(volatile int*)err) {
+        if (++spins > spin_limit || *(volatile int*)err) {
           atomicExch(err, 1);
           ok = 0;
           break;

@@ -66,7 +66,9 @@ struct ResState {
   int stop;       // set when the loop has converged or reached loop_max
   int p_pending;  // calc_p of the current iteration still to run
   int converged;
-  int pad;
+  int check;       // stop on a breakdown (p.w <= 0 or not finite, r.z not finite)
+  int breakdown;   // 0, or 1 (p.w) / 2 (r.z) with check set
+  int breakdown_n; // the iteration it happened in
   double rr_true;  // r.r of the last iteration (true-residual exit only)
   double* alphas;  // indexed by iteration number n
   double* betas;
@@ -124,6 +126,12 @@ struct Chunk {
   cudaGraphExec_t res_ppcg_graph = nullptr;  // resident PPCG iterations
   std::vector<double> res_ppcg_key;          // theta, coefficients, form of it
   int resident_mode = 0;               // 0 auto, 1 graph replay, 2 persistent
+  int solver_checks = 0;               // next resident loop: stop on a breakdown
+  // grid barrier of the persistent loop: polls before it gives up, and the
+  // arrivals it waits for beyond the grid (nonzero only to test the time-out)
+  long long barrier_spin_limit = 1LL << 26;
+  int barrier_extra = 0;
+  int res_breakdown = 0, res_breakdown_n = 0;  // what the last one found
   cudaGraphExec_t res_graph = nullptr;
   int res_graph_iters = 0;
   bool res_graph_true_exit = false;

@@ -1171,7 +1171,8 @@ static int tile_grid(Chunk& c, void (*kernel)(KArgs...), int ns = 0) {
 // L2 (CG = true).  Results are those of the three-kernel loop.
 template <int TH, int F>
 __global__ void __launch_bounds__(kBlock)
-    k_cg_persistent(Dev d, Red red, ResState* st, unsigned int* bar, int* err) {
+    k_cg_persistent(Dev d, Red red, ResState* st, unsigned int* bar, int* err,
+                    long long spin_limit, unsigned int extra_arrivals) {
   __shared__ double sh[16];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   Red rw = red, ru = red;
@@ -1195,13 +1196,13 @@ __global__ void __launch_bounds__(kBlock)
     phase(rw, [&](int x, int y0, bool xin, double* acc) {
       cg_w_tile<TH, F, true>(d, x, y0, xin, acc);
     }, true);
-    if (!grid_barrier(bar, err)) return;
+    if (!grid_barrier(bar, err, spin_limit, extra_arrivals)) return;
     const double pw = block_final_value(rw.partials, d.ns, sh);
     const double alpha = rro / pw;
     phase(ru, [&](int x, int y0, bool xin, double* acc) {
       cg_ur_tile<TH, F, 1, true>(d, x, y0, xin, acc, alpha);
     }, true);
-    if (!grid_barrier(bar, err)) return;
+    if (!grid_barrier(bar, err, spin_limit, extra_arrivals)) return;
     const double rrn = block_final_value(ru.partials, d.ns, sh);
     const double beta = rrn / rro;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1212,7 +1213,7 @@ __global__ void __launch_bounds__(kBlock)
     phase(rw, [&](int x, int y0, bool xin, double* acc) {
       cg_p_tile<TH, F, true>(d, x, y0, xin, beta);
     }, false);
-    if (!grid_barrier(bar, err)) return;
+    if (!grid_barrier(bar, err, spin_limit, extra_arrivals)) return;
   }
 }
 
@@ -1228,7 +1229,9 @@ static bool launch_cg_persistent_t(Chunk& c) {
   ResState* st = c.res_state;
   unsigned int* bar = c.res_bar;
   int* err = (int*)(c.res_bar + 2);
-  void* args[] = {&d, &red, &st, &bar, &err};
+  long long spin_limit = c.barrier_spin_limit;
+  unsigned int extra = (unsigned int)c.barrier_extra;
+  void* args[] = {&d, &red, &st, &bar, &err, &spin_limit, &extra};
   return check_cuda(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kBlock), args, 0,
                                                 c.stream),
                     "persistent CG launch");
@@ -1445,6 +1448,7 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
   h.eps_target = eps_target;
   h.n = n_begin;
   h.loop_max = loop_max;
+  h.check = c.solver_checks;
   h.alphas = c.res_coef;
   h.betas = c.res_coef + c.res_coef_n;
   if (!check_cuda(cudaMemcpyAsync(c.res_state, &h, sizeof(ResState),
@@ -1518,6 +1522,8 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
   c.res_last_rr_true = h.rr_true;
   *n_done = h.n;
   *converged = h.converged;
+  c.res_breakdown = h.breakdown;
+  c.res_breakdown_n = h.breakdown_n;
   if (cg_alphas && cg_betas) {
     const int n = h.n - n_begin + 1;
     cudaMemcpyAsync(cg_alphas + n_begin, c.res_coef + n_begin, n * sizeof(double),
@@ -1567,6 +1573,7 @@ int resident_ppcg_iterations(int n_begin, int loop_max, double rro_in,
   h.eps_target = eps_target;
   h.n = n_begin;
   h.loop_max = loop_max;
+  h.check = c.solver_checks;
   if (!check_cuda(cudaMemcpyAsync(c.res_state, &h, sizeof(ResState),
                                   cudaMemcpyHostToDevice, c.stream),
                   "resident state upload"))
@@ -1609,6 +1616,8 @@ int resident_ppcg_iterations(int n_begin, int loop_max, double rro_in,
   *error_out = h.error;
   *n_done = h.n;
   *converged = h.converged;
+  c.res_breakdown = h.breakdown;
+  c.res_breakdown_n = h.breakdown_n;
   return 0;
 }
 

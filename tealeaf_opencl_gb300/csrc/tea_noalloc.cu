@@ -49,7 +49,9 @@ __global__ void __launch_bounds__(kBlock)
 
 // Device address of the scratch array, looked up once per device.  The
 // array's name in host code is only a stand-in for the symbol, never a
-// usable address.
+// usable address.  The table is filled without locking: the first call on
+// each device should come from one host thread (two threads racing there
+// would both store the same address).
 static double* g_scratch_addr[64] = {nullptr};
 
 static double* scratch_for_current_device() {
@@ -73,8 +75,10 @@ template <int TH, int F>
 static int launch_dot_noalloc(const Dev& d, const Red& red, const double* a,
                               const double* b, cudaStream_t s) {
   int dev = 0, sms = 0, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (!check_cuda(cudaGetDevice(&dev), "tea_gb300_dot_noalloc: cudaGetDevice") ||
+      !check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
+                  "tea_gb300_dot_noalloc: SM count"))
+    return -1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
           &per_sm, k_dot_noalloc<TH, F>, kBlock, 0) != cudaSuccess ||
       per_sm < 1)
@@ -113,9 +117,10 @@ extern "C" int tea_gb300_dot_noalloc(const double* a, const double* b,
   d.ns = d.nsx * d.nty;
   if ((long long)d.nsx * d.nty > kNoAllocMaxPartials) {
     fail(32,
-         "tea_gb300_dot_noalloc: a %d x %d interior needs %lld partial sums, "
-         "which exceeds the fixed scratch of %lld (at most 16384 x 16384 cells)",
-         x_max, y_max, (long long)d.nsx * d.nty, kNoAllocMaxPartials);
+         "tea_gb300_dot_noalloc: a %d x %d interior has %lld supertiles "
+         "(ceil(ceil(x/32)/8) x ceil(y/%d)), more than the %lld partial sums "
+         "of the fixed scratch (16384 x 16384 cells fit)",
+         x_max, y_max, (long long)d.nsx * d.nty, TH, kNoAllocMaxPartials);
     return -1;
   }
   double* scratch = scratch_for_current_device();

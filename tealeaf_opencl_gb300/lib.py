@@ -18,6 +18,8 @@ SOLVER = dict(jacobi=1, cg=2, chebyshev=3, ppcg=4)
 EXTERNAL_FACE = -1
 DRIVER_PER_CALL = 0
 DRIVER_RESIDENT = 1
+CHECK_BREAKDOWN = 1  # TEA_CHECK_BREAKDOWN
+CHECK_MAX_ITERS = 2  # TEA_CHECK_MAX_ITERS
 
 # the C-ABI entry points declared in include/tealeaf_gb300.h
 REFERENCE_SYMBOLS = [
@@ -34,7 +36,7 @@ REFERENCE_SYMBOLS = [
 ]
 EXTRA_SYMBOLS = [
     "tea_gb300_configure", "tea_gb300_set_arithmetic", "tea_gb300_get_arithmetic",
-    "tea_gb300_set_resident_mode",
+    "tea_gb300_set_resident_mode", "tea_gb300_set_barrier_limits",
     "tea_gb300_set_abort_on_error", "tea_gb300_last_error",
     "tea_gb300_finalise", "tea_gb300_read_field", "tea_gb300_write_field",
     "tea_gb300_read_field_padded", "tea_gb300_write_field_padded",
@@ -42,9 +44,10 @@ EXTRA_SYMBOLS = [
     "tea_gb300_chunk_info", "tea_gb300_event_record", "tea_gb300_event_elapsed_ms",
     "tea_gb300_synchronize", "tea_gb300_host_alloc", "tea_gb300_host_free",
     "tea_gb300_kernel_timer_select", "tea_gb300_kernel_timer_read",
-    "tea_gb300_kernel_timer_read_name", "tea_gb300_fp64_rate",
+    "tea_gb300_kernel_timer_read_name", "tea_gb300_fp64_rate", "tea_gb300_emu_check",
     "tea_gb300_dot_noalloc", "tea_gb300_mixed_solve", "tea_gb300_mixed_solve_ppcg",
     "tea_gb300_driver_open", "tea_gb300_driver_step", "tea_gb300_driver_close",
+    "tea_gb300_driver_set_limits",
     "tea_gb300_batch_create", "tea_gb300_batch_set_fields", "tea_gb300_batch_run",
     "tea_gb300_batch_summary", "tea_gb300_batch_iterations",
     "tea_gb300_batch_read_field", "tea_gb300_batch_set_launch",
@@ -63,6 +66,7 @@ class StepInfo(C.Structure):
         ("ie", C.c_double), ("temp", C.c_double), ("complete", C.c_int),
         ("qa_passed", C.c_int), ("qa_diff", C.c_double),
         ("outer_corrections", C.c_int), ("relative_residual", C.c_double),
+        ("switch_iteration", C.c_int),
     ]
 
     def as_dict(self):
@@ -175,6 +179,7 @@ def load(build=True):
         "tea_gb300_set_arithmetic": (i, [i]),
         "tea_gb300_get_arithmetic": (i, []),
         "tea_gb300_set_resident_mode": (i, [i]),
+        "tea_gb300_set_barrier_limits": (i, [C.c_longlong, i]),
         "tea_gb300_last_error": (i, [C.c_char_p, i]),
         "tea_gb300_finalise": (v, []),
         "tea_gb300_read_field": (i, [i, PD]),
@@ -194,6 +199,8 @@ def load(build=True):
         "tea_gb300_kernel_timer_read": (i, [PD, C.POINTER(C.c_longlong)]),
         "tea_gb300_kernel_timer_read_name": (i, [C.c_char_p, PD, C.POINTER(C.c_longlong)]),
         "tea_gb300_fp64_rate": (d, []),
+        "tea_gb300_emu_check": (i, [i, C.c_void_p, C.c_void_p, C.c_longlong, d,
+                                    C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
         "tea_gb300_dot_noalloc": (i, [C.c_void_p, C.c_void_p, i, i, i, C.c_longlong,
                                       C.c_void_p, C.c_void_p]),
         "tea_gb300_mixed_solve": (i, [d, d, i, i, C.POINTER(MixedInfo)]),
@@ -201,6 +208,7 @@ def load(build=True):
         "tea_gb300_driver_open": (i, [C.c_char_p, C.c_char_p, i, i]),
         "tea_gb300_driver_step": (i, [C.POINTER(StepInfo)]),
         "tea_gb300_driver_close": (v, []),
+        "tea_gb300_driver_set_limits": (i, [i, i]),
         "tea_gb300_batch_create": (i, [i, PI, PI, d, d, d, d, i, i]),
         "tea_gb300_batch_set_fields": (i, [i, PD, PD]),
         "tea_gb300_batch_run": (i, [i, d, d, i, C.POINTER(BatchStats)]),
@@ -254,11 +262,11 @@ def _pi(a):
 class Chunk:
     """The process-global chunk, driven through the reference's entry points."""
 
-    def __init__(self, x_max, y_max, halo=1, solver="cg", prec="none"):
+    def __init__(self, x_max, y_max, halo=1, solver="cg", prec="none", profiler=False):
         L = load()
         s = SOLVER[solver] if isinstance(solver, str) else int(solver)
         p = PREC[prec] if isinstance(prec, str) else int(prec)
-        if L.tea_gb300_configure(int(halo), s, p, 0) != 0:
+        if L.tea_gb300_configure(int(halo), s, p, 1 if profiler else 0) != 0:
             raise TeaError("invalid configuration")
         L.initialise_ocl_(_ip(1), _ip(x_max), _ip(1), _ip(y_max))
         check()
@@ -436,7 +444,8 @@ def write_field(name, arr):
 class Driver:
     """The whole-run driver: tea.in text in, one timestep per step()."""
 
-    def __init__(self, deck_text, mode=DRIVER_PER_CALL, max_iters_cap=0, log_path=None):
+    def __init__(self, deck_text, mode=DRIVER_PER_CALL, max_iters_cap=0, log_path=None,
+                 cap_after_switch=0, checks=0):
         L = load()
         rc = L.tea_gb300_driver_open(deck_text.encode(),
                                      log_path.encode() if log_path else None,
@@ -444,6 +453,10 @@ class Driver:
         if rc != 0:
             check()
             raise TeaError("driver_open failed")
+        if (cap_after_switch or checks) and \
+                L.tea_gb300_driver_set_limits(int(cap_after_switch), int(checks)) != 0:
+            check()
+            raise TeaError("driver_set_limits failed")
 
     def step(self):
         info = StepInfo()
@@ -457,9 +470,10 @@ class Driver:
         load().tea_gb300_driver_close()
 
 
-def run_deck(deck_text, mode=DRIVER_PER_CALL, max_iters_cap=0, log_path=None):
+def run_deck(deck_text, mode=DRIVER_PER_CALL, max_iters_cap=0, log_path=None,
+             cap_after_switch=0, checks=0):
     """Run a deck to completion; returns the list of per-step StepInfo."""
-    drv = Driver(deck_text, mode, max_iters_cap, log_path)
+    drv = Driver(deck_text, mode, max_iters_cap, log_path, cap_after_switch, checks)
     steps = []
     try:
         while True:

@@ -1,12 +1,23 @@
-"""Records the CPU oracle's results for the long CG test problems.
+"""Records the CPU oracle's results for runs too long for the CPU test suite.
 
-tests/test_gpu_runs.py compares the GPU runs of test problems 2 and 3
-(960^2 and 3840^2 CG, tens of thousands of iterations) with these records
-bit for bit: per-step iteration counts and the final temperature (as a hex
-float).  The oracle takes minutes to hours on a CPU for these, so the
-results are kept as a fixture: oracle_pins.json for the exact arithmetic
-form, oracle_pins_fused.json and oracle_pins_chain.json for the others.
-Usage: make_oracle_pins.py [--fused | --chain] TP [TP ...]
+Test problems.  tests/test_gpu_runs.py compares the GPU runs of test
+problems 2 and 3 (960^2 and 3840^2 CG, tens of thousands of iterations)
+with these records bit for bit: per-step iteration counts and the final
+temperature (as a hex float).  The oracle takes minutes to hours on a CPU
+for these, so the results are kept as a fixture: oracle_pins.json for the
+exact arithmetic form, oracle_pins_fused.json and oracle_pins_chain.json
+for the others.
+
+    make_oracle_pins.py [--fused | --chain] TP [TP ...]
+
+Benchmark workloads.  tests/test_gpu_headline.py runs the benchmark's own
+4096^2 decks (bench.py's deck_for: five states, block Jacobi, halo depth 2,
+20 CG steps before the switch, tl_eps 1e-15) for two timesteps, each ended
+CAP iterations after its switch from CG to PPCG or Chebyshev, and compares
+them with these records bit for bit.  The deck text is stored with the
+record, so the pin says exactly what it pins.
+
+    make_oracle_pins.py --workload ppcg4096|cheby4096 [--exact|--chain] [--cap N]
 """
 import json
 import os
@@ -14,9 +25,50 @@ import sys
 import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
 
 from oracle import oracle  # noqa: E402
+
+HEADLINE_FILE = os.path.join(HERE, "oracle_pins_headline.json")
+HEADLINE_STEPS = 2
+HEADLINE_CAP = 20
+
+
+def headline_deck(workload, form, steps=HEADLINE_STEPS):
+    """The deck bench.py times for `workload`, in arithmetic form `form`."""
+    import bench
+    saved = bench.ARITHMETIC
+    try:
+        bench.ARITHMETIC = form
+        return bench.deck_for(workload, steps)
+    finally:
+        bench.ARITHMETIC = saved
+
+
+def pin_headline(workload, form, cap):
+    pins = json.load(open(HEADLINE_FILE)) if os.path.exists(HEADLINE_FILE) else {}
+    deck = headline_deck(workload, form)
+    t0 = time.time()
+    res = oracle.run_deck(deck, max_after_switch=cap)
+    n = res.n_steps
+    final = res.summaries()[-1]
+    pins["%s/%s" % (workload, form)] = {
+        "workload": workload,
+        "arithmetic": form,
+        "deck": deck,
+        "cap_after_switch": cap,
+        "iterations": list(res.iterations[:n]),
+        "inner_iterations": list(res.inner_iterations[:n]),
+        "switch_iteration": list(res.switch_iteration[:n]),
+        "summary_hex": {k: float(final[i]).hex()
+                        for k, i in (("vol", 1), ("mass", 2), ("ie", 4), ("temp", 5))},
+        "oracle_threads": oracle.lib().oracle_num_threads(),
+        "oracle_seconds": round(time.time() - t0, 1),
+    }
+    json.dump(pins, open(HEADLINE_FILE, "w"), indent=1, sort_keys=True)
+    print(workload, form, list(res.iterations[:n]), list(res.switch_iteration[:n]),
+          final[5], flush=True)
 
 
 def main(tps, form):
@@ -48,4 +100,9 @@ def main(tps, form):
 if __name__ == "__main__":
     args = sys.argv[1:]
     form = "fused" if "--fused" in args else "chain" if "--chain" in args else "exact"
-    main([int(a) for a in args if not a.startswith("--")] or [2], form)
+    if "--workload" in args:
+        wl = args[args.index("--workload") + 1]
+        cap = int(args[args.index("--cap") + 1]) if "--cap" in args else HEADLINE_CAP
+        pin_headline(wl, form, cap)
+    else:
+        main([int(a) for a in args if not a.startswith("--")] or [2], form)

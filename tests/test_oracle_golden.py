@@ -78,3 +78,55 @@ def test_arithmetic_forms_agree_within_tolerance(other, solver, prec):
     sa, sb = a.summaries()[-1], b.summaries()[-1]
     assert max(abs(sa[i] - sb[i]) / abs(sa[i]) for i in (1, 2, 4, 5)) < 1e-12
     assert all(abs(a.iterations[i] - b.iterations[i]) <= 1 for i in range(5))
+
+
+HEADLINE_PINS = os.path.join(GOLD, "oracle_pins_headline.json")
+
+
+@pytest.mark.parametrize("workload", ["ppcg4096", "cheby4096"])
+def test_headline_pins_are_the_bench_decks_and_forms_agree(workload):
+    """The oracle pins of the benchmark's 4096^2 decks (recorded by
+    make_oracle_pins.py) hold the exact deck bench.py times, in the exact
+    and chain forms; on the oracle the two forms agree to 1e-12 in the
+    field summary and to 1 in every iteration count."""
+    import bench
+    pins = json.load(open(HEADLINE_PINS))
+    got = {}
+    for form in ("exact", "chain"):
+        p = pins["%s/%s" % (workload, form)]
+        saved = bench.ARITHMETIC
+        bench.ARITHMETIC = form
+        try:
+            assert p["deck"] == bench.deck_for(workload, len(p["iterations"]))
+        finally:
+            bench.ARITHMETIC = saved
+        assert p["switch_iteration"][0] >= 20  # past the CG pre-steps
+        assert all(s > 0 for s in p["switch_iteration"])
+        got[form] = p
+    a, b = got["exact"], got["chain"]
+    assert all(abs(x - y) <= 1 for x, y in zip(a["iterations"], b["iterations"]))
+    for k, v in a["summary_hex"].items():
+        x, y = float.fromhex(v), float.fromhex(b["summary_hex"][k])
+        assert abs(x - y) <= 1e-12 * abs(x), k
+
+
+@pytest.mark.parametrize("solver", ["ppcg", "chebyshev"])
+def test_cap_after_switch_bounds_the_polynomial_phase(solver):
+    """max_after_switch ends a step that many iterations after its switch,
+    the switch's own iteration counted; steps after the first PPCG step
+    switch at iteration 2 (tea_solve.f90:153-155)."""
+    from tealeaf_opencl_gb300 import decks
+    deck = decks.five_state_deck(64, solver=solver, prec="jac_block", steps=3, eps=1e-15,
+                                 halo=2, inner_steps=10, presteps=20, summary_frequency=0)
+    full = oracle.run_deck(deck)
+    cap = 3
+    res = oracle.run_deck(deck, max_after_switch=cap)
+    for i in range(3):
+        sw = res.switch_iteration[i]
+        assert sw >= (20 if (i == 0 or solver == "chebyshev") else 2)
+        assert res.iterations[i] == sw - 1 + cap
+        if solver == "ppcg":
+            assert res.inner_iterations[i] == 10 * cap
+    assert res.switch_iteration[0] == full.switch_iteration[0]
+    if solver == "ppcg":
+        assert list(res.switch_iteration[1:3]) == [2, 2]
