@@ -252,6 +252,8 @@ struct Config {
   int halo = 1, solver = SOLVER_JACOBI, prec = PREC_NONE, profiler = 0;
   int arith = 1;  // arithmetic form
   int resident_mode = 0;
+  long long barrier_spin_limit = 1LL << 26;  // persistent loop's grid barrier
+  int barrier_extra = 0;
 };
 static Config g_config;
 
@@ -327,6 +329,8 @@ static bool init_chunk(int x_max, int y_max, const Config& cfg) {
   c.profiler_on = cfg.profiler != 0;
   c.arith = cfg.arith;
   c.resident_mode = cfg.resident_mode;
+  c.barrier_spin_limit = cfg.barrier_spin_limit;
+  c.barrier_extra = cfg.barrier_extra;
   c.TH = reduction_rows(x_max, y_max);
   c.S = ((long long)(x_max + 2 * c.H + 1 + 31) / 32) * 32;
   c.rows = y_max + 2 * c.H + 1;
@@ -827,8 +831,8 @@ extern "C" int tea_gb300_set_barrier_limits(long long spin_limit, int extra_arri
          extra_arrivals);
     return -1;
   }
-  chunk().barrier_spin_limit = spin_limit;
-  chunk().barrier_extra = extra_arrivals;
+  g_config.barrier_spin_limit = chunk().barrier_spin_limit = spin_limit;
+  g_config.barrier_extra = chunk().barrier_extra = extra_arrivals;
   return 0;
 }
 

@@ -85,6 +85,44 @@ __device__ __forceinline__ double mul_e(double a, double b) {
 // to 214 us (fused) at 4096^2.  Kernels with high register pressure (the
 // Chebyshev step) keep EMU off: the extra registers cost them more than the
 // FP64 instructions saved.
+// The operator on values: diagonal D, face coefficients Ky_n (Ky of the
+// row above), Ky_c, Kx_e (Kx of the column to the right), Kx_c, and x at
+// the cell and its north, south, east and west neighbours.
+template <int F, bool EMU = true>
+__device__ __forceinline__ double smvp_v(double D, double kyn, double kyc, double kxe,
+                                         double kxc, double xc, double xn, double xs,
+                                         double xe, double xw) {
+  if (!F) return D * xc - (mul_e<EMU>(kyn, xn) + kyc * xs) - (mul_e<EMU>(kxe, xe) + kxc * xw);
+  if (F == 2) {
+    double t = mul_e<EMU>(D, xc);
+    t = __fma_rn(-kyn, xn, t);
+    t = __fma_rn(-kyc, xs, t);
+    t = __fma_rn(-kxe, xe, t);
+    return __fma_rn(-kxc, xw, t);
+  }
+  const double t1 = __fma_rn(kyc, xs, mul_e<EMU>(kyn, xn));
+  const double t2 = __fma_rn(kxc, xw, mul_e<EMU>(kxe, xe));
+  return __fma_rn(D, xc, -t1) - t2;
+}
+
+// b - A x on values: the reference's "b - smvp" (calc_residual,
+// tea_leaf_common_cl.cl:17-36; ppcg update_r, tea_leaf_ppcg_cl.cl:62-88),
+// or in the chain form the chain of fused multiply-adds started from b.
+template <int F>
+__device__ __forceinline__ double bms_v(double b, double D, double kyn, double kyc,
+                                        double kxe, double kxc, double xc, double xn,
+                                        double xs, double xe, double xw) {
+  if (F != 2) return b - smvp_v<F>(D, kyn, kyc, kxe, kxc, xc, xn, xs, xe, xw);
+  double t = __fma_rn(-D, xc, b);
+  t = __fma_rn(kyn, xn, t);
+  t = __fma_rn(kyc, xs, t);
+  t = __fma_rn(kxe, xe, t);
+  return __fma_rn(kxc, xw, t);
+}
+
+// The same operator at offset c of the padded fields, written out with the
+// loads in place (the kernels' register budgets were tuned on this form);
+// its arithmetic is smvp_v's.
 template <int F, bool CG = false, bool EMU = true>
 __device__ __forceinline__ double smvp(const Dev& d, const double* x,
                                        long long c) {
@@ -108,9 +146,7 @@ __device__ __forceinline__ double smvp(const Dev& d, const double* x,
   return __fma_rn(D, ldv<CG>(x + c), -t1) - t2;
 }
 
-// b - A x at offset c: the reference's "b - smvp" (calc_residual,
-// tea_leaf_common_cl.cl:17-36; ppcg update_r, tea_leaf_ppcg_cl.cl:62-88),
-// or in the chain form the chain of fused multiply-adds started from b.
+// b - A x at offset c (the arithmetic of bms_v)
 template <int F>
 __device__ __forceinline__ double b_minus_smvp(const Dev& d, const double* x,
                                                long long c, double b) {
@@ -161,6 +197,44 @@ __device__ __forceinline__ double bwd(double dp, double cp, double z) {
 // block_solve_func (tea_block_jacobi.cl:6-42) for one column of one strip:
 // z = M_block^-1 r for the strip whose first cell is at offset c0.  With
 // EMU the multiplies by bfp run on the integer pipes (same bits).
+// The strip solve on values: bfp, Ky and cp of the strip's rows 0..3 (Ky of
+// row 0 and cp of row 3 unused), diag of row 0 (exact form only); entries of
+// rows at or past `upper` are not read.
+template <int F, bool EMU = false>
+__device__ __forceinline__ void strip_solve_v(int upper, const double rl[4],
+                                              const double bfp[4], const double ky[4],
+                                              const double cp[4], double diag0,
+                                              double zl[4]) {
+  double dp0, dp1 = 0.0, dp2 = 0.0, dp3 = 0.0;
+  dp0 = F ? mul_e<EMU>(rl[0], bfp[0]) : emu_ddiv_var(rl[0], diag0);
+  if (upper > 1) dp1 = fwd<F, EMU>(rl[1], ky[1], dp0, bfp[1]);
+  if (upper > 2) dp2 = fwd<F, EMU>(rl[2], ky[2], dp1, bfp[2]);
+  if (upper > 3) dp3 = fwd<F, EMU>(rl[3], ky[3], dp2, bfp[3]);
+  double z0, z1 = 0.0, z2 = 0.0, z3 = 0.0;
+  if (upper == 4) {
+    z3 = dp3;
+    z2 = bwd<F>(dp2, cp[2], z3);
+    z1 = bwd<F>(dp1, cp[1], z2);
+    z0 = bwd<F>(dp0, cp[0], z1);
+  } else if (upper == 3) {
+    z2 = dp2;
+    z1 = bwd<F>(dp1, cp[1], z2);
+    z0 = bwd<F>(dp0, cp[0], z1);
+  } else if (upper == 2) {
+    z1 = dp1;
+    z0 = bwd<F>(dp0, cp[0], z1);
+  } else {
+    z0 = dp0;
+  }
+  zl[0] = z0;
+  zl[1] = z1;
+  zl[2] = z2;
+  zl[3] = z3;
+}
+
+// The strip solve at offset c0 of the padded fields (the arithmetic of
+// strip_solve_v, with the loads in place; only the rows the strip has are
+// read, since a strip may end at the top of the allocation).
 template <int F, bool EMU = false>
 __device__ __forceinline__ void strip_solve(const Dev& d, long long c0,
                                             int upper, const double rl[4],

@@ -53,7 +53,8 @@ def test_problem_1_log_has_the_reference_layout(tmp_path):
     assert len(qa) == 1
     assert re.match(r"^Test problem   1 is within {3}0\.\d{7}E[+-]\d{2}% of the expected "
                     r"solution$", qa[0]), repr(qa[0])
-    assert abs(fortran_float(qa[0][26:42]) - last.qa_diff) <= 1e-7 * last.qa_diff
+    # e16.7 keeps 7 significant digits
+    assert abs(fortran_float(qa[0][26:42]) - last.qa_diff) <= 5e-7 * last.qa_diff
     assert " This test is considered PASSED" in text
     its = [int(ln[16:]) for ln in text if ln.startswith("Iteration count ")]
     assert its == [s.iterations - 1 for s in steps] or its == [s.iterations for s in steps]
@@ -73,7 +74,8 @@ def test_ppcg_log_reports_the_switch_in_the_reference_layout(tmp_path):
     sw = [ln for ln in text if ln.startswith("Switching after")]
     assert len(sw) == 2
     # '(a,i3,a,e15.7)': "Switching after ", i3, " CG its, error ", e15.7
-    m = re.match(r"^Switching after([ \d]{3}) CG its, error ( {2}0\.\d{7}E[+-]\d{2})$", sw[0])
+    # (13 characters for a positive value, two blanks before it)
+    m = re.match(r"^Switching after ([ \d]{3}) CG its, error ( {2}0\.\d{7}E[+-]\d{2})$", sw[0])
     assert m, repr(sw[0])
     assert int(m.group(1)) == steps[0].switch_iteration
     eig = [ln for ln in text if ln.startswith("Eigen min")]

@@ -80,8 +80,11 @@ def test_dot_noalloc_rejects_interior_beyond_scratch():
     L = lib.load()
     buf = ctypes.c_double(0.0)
     p = ctypes.addressof(buf)
-    rc = L.tea_gb300_dot_noalloc(p, p, 20000, 20000, 1, 20002, p, None)
-    assert rc == -1
-    msg = ctypes.create_string_buffer(512)
-    assert L.tea_gb300_last_error(msg, 512) != 0
-    assert b"exceeds the fixed scratch" in msg.value
+    # the bound is on supertiles (8 x 32 columns by 16 rows here), not on
+    # the side length: a wide square and a thin, tall strip both exceed it
+    for x, y in ((20000, 20000), (32, 2_200_000)):
+        rc = L.tea_gb300_dot_noalloc(p, p, x, y, 1, x + 2, p, None)
+        assert rc == -1
+        msg = ctypes.create_string_buffer(512)
+        assert L.tea_gb300_last_error(msg, 512) != 0
+        assert b"partial sums of the fixed scratch" in msg.value
