@@ -229,6 +229,11 @@ static void free_chunk(Chunk& c) {
   free(c.ppcg_alpha_h);
   free(c.ppcg_beta_h);
   c.cheby_alpha_h = c.cheby_beta_h = c.ppcg_alpha_h = c.ppcg_beta_h = nullptr;
+  cudaFree(c.r2.base);
+  cudaFree(c.sd2.base);
+  c.r2 = c.sd2 = Field();
+  c.pending_inner = -1;
+  tb_release();
   if (c.stream) cudaStreamDestroy(c.stream);
   c.stream = nullptr;
   c.ready = false;
@@ -376,12 +381,41 @@ static bool init_chunk(int x_max, int y_max, const Config& cfg) {
   return check_cuda(cudaStreamSynchronize(c.stream), "chunk allocation");
 }
 
+// Every entry point that works on the chunk first launches a PPCG inner step
+// held back for pairing (flush_pending_inner), so what any call sees is
+// what the reference's call sequence would have produced by then.
 static bool need_chunk(const char* who) {
   if (!chunk().ready) {
     fail(5, "%s called before initialise_ocl_", who);
     return false;
   }
+  flush_pending_inner(chunk());
   return true;
+}
+
+bool ensure_alt_fields(Chunk& c) {
+  if (c.r2.base) return true;
+  if (!alloc_field(c, c.r2) || !alloc_field(c, c.sd2)) return false;
+  // the halos (never written by the solve) must match the live pair's
+  const size_t n = (size_t)((32 - (c.H % 32)) % 32 + c.rows * c.S + 32) * sizeof(double);
+  return check_cuda(cudaMemcpyAsync(c.r2.base, c.r.base, n, cudaMemcpyDeviceToDevice, c.stream),
+                    "alt r copy") &&
+         check_cuda(cudaMemcpyAsync(c.sd2.base, c.sd.base, n, cudaMemcpyDeviceToDevice, c.stream),
+                    "alt sd copy");
+}
+
+void swap_alt_fields(Chunk& c) {
+  std::swap(c.r, c.r2);
+  std::swap(c.sd, c.sd2);
+  c.field_epoch++;
+}
+
+void flush_pending_inner(Chunk& c) {
+  const int s = c.pending_inner;
+  if (s < 0) return;
+  c.pending_inner = -1;
+  launch_ppcg_update_r(c);
+  launch_ppcg_calc_sd(c, c.ppcg_alpha_h[s], c.ppcg_beta_h[s]);
 }
 
 // The next reduction launched copies its result to mapped host memory and
@@ -708,10 +742,14 @@ extern "C" void tea_leaf_ppcg_inner_kernel_ocl_(int* inner_step,
                                                 int* bounds_extra,
                                                 const int* chunk_neighbours) {
   (void)bounds_extra;
-  if (!need_chunk("tea_leaf_ppcg_inner_kernel_ocl_")) return;
   Chunk& c = chunk();
+  if (!c.ready) {
+    fail(5, "tea_leaf_ppcg_inner_kernel_ocl_ called before initialise_ocl_");
+    return;
+  }
   for (int f = 0; f < 4; f++) {
     if (chunk_neighbours[f] != TEA_EXTERNAL_FACE) {
+      flush_pending_inner(c);
       fail(7, "tea_leaf_ppcg_inner_kernel_ocl_: only a single chunk (all "
               "faces external) is supported");
       return;
@@ -719,10 +757,31 @@ extern "C" void tea_leaf_ppcg_inner_kernel_ocl_(int* inner_step,
   }
   const int s = *inner_step - 1;
   if (s < 0 || s >= c.n_ppcg) {
+    flush_pending_inner(c);
     fail(11, "PPCG inner step %d outside the %d stored coefficients",
          *inner_step, c.n_ppcg);
     return;
   }
+  // Steps are paired: a step that a later one may follow is held back, and
+  // when the next step arrives the two run as one fused pass
+  // (tea_ppcg_tb.cu); any other call launches a held step first.  The
+  // results are those of one update_r + calc_sd per call.
+  if (tb_applicable(c)) {
+    if (c.pending_inner >= 0 && c.pending_inner == s - 1) {
+      c.pending_inner = -1;
+      if (!ensure_alt_fields(c) ||
+          !launch_ppcg_inner_pair(c, s - 1, nullptr, c.r.f, c.sd.f, c.r2.f, c.sd2.f))
+        return;
+      swap_alt_fields(c);
+      return;
+    }
+    flush_pending_inner(c);
+    if (s + 1 < c.n_ppcg) {
+      c.pending_inner = s;
+      return;
+    }
+  }
+  flush_pending_inner(c);
   launch_ppcg_update_r(c);
   launch_ppcg_calc_sd(c, c.ppcg_alpha_h[s], c.ppcg_beta_h[s]);
 }
@@ -807,6 +866,7 @@ extern "C" int tea_gb300_set_arithmetic(int form) {
          form);
     return -1;
   }
+  if (chunk().ready) flush_pending_inner(chunk());  // a held step keeps its form
   g_config.arith = form;
   chunk().arith = form;
   return 0;
@@ -871,6 +931,14 @@ static int copy_field(int id, double* host, const double* in, bool padded) {
                           w * sizeof(double), h, cudaMemcpyDeviceToHost,
                           c.stream);
   if (!check_cuda(e, "field copy")) return -1;
+  // the second r/sd buffer keeps the same halo (the fused PPCG inner steps
+  // read halos from whichever buffer is live)
+  Field* alt = f == &c.r ? &c.r2 : f == &c.sd ? &c.sd2 : nullptr;
+  if (in && padded && alt && alt->base &&
+      !check_cuda(cudaMemcpy2DAsync(alt->f, c.S * sizeof(double), in, w * sizeof(double),
+                                    w * sizeof(double), h, cudaMemcpyHostToDevice, c.stream),
+                  "field copy (second buffer)"))
+    return -1;
   // the stored diagonal follows the face coefficients
   if (in && (id == 12 || id == 13)) launch_init_diag(c);
   return check_cuda(cudaStreamSynchronize(c.stream), "field copy sync") ? 0 : -1;
@@ -895,7 +963,10 @@ extern "C" int tea_gb300_reduction_rows(int x_max, int y_max) {
 
 extern "C" long long tea_gb300_kernel_launches(void) { return g_launches; }
 
-extern "C" void* tea_gb300_stream(void) { return (void*)chunk().stream; }
+extern "C" void* tea_gb300_stream(void) {
+  if (chunk().ready) flush_pending_inner(chunk());
+  return (void*)chunk().stream;
+}
 
 extern "C" int tea_gb300_chunk_info(int* x_max, int* y_max, int* halo,
                                     int* stride) {
@@ -913,6 +984,7 @@ static cudaEvent_t g_events[16] = {nullptr};
 extern "C" int tea_gb300_event_record(int slot) {
   Chunk& c = chunk();
   if (slot < 0 || slot >= 16 || !c.ready) return -1;
+  flush_pending_inner(c);
   if (!g_events[slot] && !check_cuda(cudaEventCreate(&g_events[slot]), "cudaEventCreate"))
     return -1;
   return check_cuda(cudaEventRecord(g_events[slot], c.stream), "cudaEventRecord") ? 0 : -1;
@@ -930,6 +1002,7 @@ extern "C" float tea_gb300_event_elapsed_ms(int a, int b) {
 extern "C" int tea_gb300_synchronize(void) {
   Chunk& c = chunk();
   if (!c.ready) return -1;
+  flush_pending_inner(c);
   return check_cuda(cudaStreamSynchronize(c.stream), "cudaStreamSynchronize") ? 0 : -1;
 }
 

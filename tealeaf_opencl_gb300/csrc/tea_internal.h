@@ -126,6 +126,12 @@ struct Chunk {
   cudaGraphExec_t res_ppcg_graph = nullptr;  // resident PPCG iterations
   std::vector<double> res_ppcg_key;          // theta, coefficients, form of it
   int resident_mode = 0;               // 0 auto, 1 graph replay, 2 persistent
+  // second r and sd buffers for the fused pair of PPCG inner steps
+  // (tea_ppcg_tb.cu), which writes r and sd to the pair it does not read;
+  // allocated on first use, with the halos of the live pair
+  Field r2, sd2;
+  int field_epoch = 0;      // bumped whenever r/sd and r2/sd2 trade places
+  int pending_inner = -1;   // a per-call inner step (0-based) not launched yet
   int solver_checks = 0;               // next resident loop: stop on a breakdown
   // grid barrier of the persistent loop: polls before it gives up, and the
   // arrivals it waits for beyond the grid (nonzero only to test the time-out)
@@ -135,6 +141,7 @@ struct Chunk {
   cudaGraphExec_t res_graph = nullptr;
   int res_graph_iters = 0;
   bool res_graph_true_exit = false;
+  int res_graph_epoch = 0;  // field_epoch the CG graph was captured at
   double res_last_rr_true = 0.0;
 
   Dev dev() const;
@@ -231,6 +238,20 @@ int resident_ppcg_iterations(int n_begin, int loop_max, double rro_in,
                              double eps_target, double* rro_out, double* error_out,
                              int* n_done, int* converged);
 void resident_release();
+// fused pair of PPCG inner steps (tea_ppcg_tb.cu)
+bool tb_applicable(const Chunk& c);
+bool tb_prepare(Chunk& c);  // before any graph capture that launches the pair
+bool launch_ppcg_inner_pair(Chunk& c, int s, const ResState* st, double* r_in,
+                            double* sd_in, double* r_out, double* sd_out);
+int tb_error();
+void tb_release();
+// the second r/sd buffers (tea_abi.cu): allocated and given the live
+// buffers' contents once; false on failure
+bool ensure_alt_fields(Chunk& c);
+// r/sd and r2/sd2 trade places (the fused pair has just written r2/sd2)
+void swap_alt_fields(Chunk& c);
+// launches a per-call PPCG inner step held back for pairing (tea_abi.cu)
+void flush_pending_inner(Chunk& c);
 // mixed-precision solve (tea_mixed.cu)
 void mixed_release();
 // eigenvalue range from CG alphas/betas (nsteps of each, iteration 1

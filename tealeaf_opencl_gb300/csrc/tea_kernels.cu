@@ -1289,8 +1289,47 @@ __global__ void __launch_bounds__(kBlock) k_ppcg_rz_step(Dev d, Red red, ResStat
   }
 }
 
+// True when the resident PPCG loop runs its inner steps in fused pairs.
+static bool resident_pairs(const Chunk& c) { return tb_applicable(c) && c.n_ppcg >= 2; }
+
 template <int TH, int F>
 static void enqueue_ppcg_iterations_t(Chunk& c, int iters) {
+  if (resident_pairs(c)) {
+    // Inner steps two at a time (tea_ppcg_tb.cu).  Each pair writes r and sd
+    // to the other buffer pair, so the sequence alternates between the two
+    // field sets; the host copies back if the loop stops on the other one.
+    Dev dv[2] = {c.dev(), c.dev()};
+    dv[1].r = c.r2.f;
+    dv[1].sd = c.sd2.f;
+    const Dev d4v[2] = {rows4_tiling(dv[0]), rows4_tiling(dv[1])};
+    const Red red = c.red();
+    ResState* st = c.res_state;
+    const DivConst theta = div_const(c.ppcg_theta);
+    const int gw = tile_grid(c, k_cg_calc_w<TH, F>);
+    const int gu = tile_grid(c, k_ppcg_ur_sd<TH, F>);
+    const int gr = tile_grid(c, k_ppcg_update_r<4, F>, d4v[0].ns);
+    const int gs = tile_grid(c, k_ppcg_calc_sd_block<4, F, kSdMinBlocks>, d4v[0].ns);
+    const int gz = tile_grid(c, k_ppcg_rz_step<TH, F>);
+    const int gp = tile_grid(c, k_cg_calc_p<4, F>, d4v[0].ns);
+    int cur = 0;
+    for (int i = 0; i < iters; i++) {
+      k_cg_calc_w<TH, F><<<gw, kBlock, 0, c.stream>>>(dv[cur], red, st);
+      k_ppcg_ur_sd<TH, F><<<gu, kBlock, 0, c.stream>>>(dv[cur], red, st, theta);
+      int k = 0;
+      for (; k + 1 < c.n_ppcg; k += 2) {
+        launch_ppcg_inner_pair(c, k, st, dv[cur].r, dv[cur].sd, dv[cur ^ 1].r, dv[cur ^ 1].sd);
+        cur ^= 1;
+      }
+      if (k < c.n_ppcg) {
+        k_ppcg_update_r<4, F><<<gr, kBlock, 0, c.stream>>>(d4v[cur], red, st);
+        k_ppcg_calc_sd_block<4, F, kSdMinBlocks><<<gs, kBlock, 0, c.stream>>>(
+            d4v[cur], red, c.ppcg_alpha_h[k], c.ppcg_beta_h[k], st);
+      }
+      k_ppcg_rz_step<TH, F><<<gz, kBlock, 0, c.stream>>>(dv[cur], red, st);
+      k_cg_calc_p<4, F><<<gp, kBlock, 0, c.stream>>>(d4v[cur], red, 0.0, st, c.res_counter);
+    }
+    return;
+  }
   const Dev d = c.dev();
   const Dev d4 = dev4(c);  // the kernels that take no sum
   const Red red = c.red();
@@ -1418,7 +1457,9 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
                            double* error_out, int* n_done, int* converged,
                            double* cg_alphas, double* cg_betas, bool true_exit) {
   Chunk& c = chunk();
-  if (c.res_graph && c.res_graph_true_exit != true_exit) {
+  flush_pending_inner(c);
+  if (c.res_graph &&
+      (c.res_graph_true_exit != true_exit || c.res_graph_epoch != c.field_epoch)) {
     cudaGraphExecDestroy(c.res_graph);
     c.res_graph = nullptr;
   }
@@ -1492,6 +1533,7 @@ int resident_cg_iterations(int n_begin, int loop_max, double rro_in,
     cudaGraphDestroy(graph);
     c.res_graph_iters = batch;
     c.res_graph_true_exit = true_exit;
+    c.res_graph_epoch = c.field_epoch;
   }
   // every batch runs at least one iteration until the loop stops, so the
   // loop needs at most this many batches; more means the state is corrupt
@@ -1560,7 +1602,11 @@ int resident_ppcg_iterations(int n_begin, int loop_max, double rro_in,
       return -1;
     cudaMemsetAsync(c.res_counter, 0, sizeof(unsigned int), c.stream);
   }
-  std::vector<double> key = {c.ppcg_theta, (double)c.arith, (double)c.n_ppcg};
+  flush_pending_inner(c);
+  const bool pairs = resident_pairs(c);
+  if (pairs && (!ensure_alt_fields(c) || !tb_prepare(c))) return -1;
+  std::vector<double> key = {c.ppcg_theta, (double)c.arith, (double)c.n_ppcg,
+                             (double)c.field_epoch, pairs ? 1.0 : 0.0};
   key.insert(key.end(), c.ppcg_alpha_h, c.ppcg_alpha_h + c.n_ppcg);
   key.insert(key.end(), c.ppcg_beta_h, c.ppcg_beta_h + c.n_ppcg);
   if (c.res_ppcg_graph && key != c.res_ppcg_key) {
@@ -1590,7 +1636,8 @@ int resident_ppcg_iterations(int n_begin, int loop_max, double rro_in,
     cudaGraphDestroy(graph);
     c.res_ppcg_key = key;
   }
-  const int per_iter = 4 + 2 * c.n_ppcg;
+  const int per_iter =
+      pairs ? 4 + c.n_ppcg / 2 + 2 * (c.n_ppcg % 2) : 4 + 2 * c.n_ppcg;
   const long long max_batches = (long long)(loop_max - n_begin) / batch + 3;
   for (long long nb = 0;; nb++) {
     if (nb >= max_batches) {
@@ -1610,7 +1657,21 @@ int resident_ppcg_iterations(int n_begin, int loop_max, double rro_in,
                     "resident state read") ||
         !check_cuda(cudaStreamSynchronize(c.stream), "resident sync"))
       return -1;
+    if (pairs && tb_error()) {
+      fail(81, "fused PPCG inner steps: a shared-memory copy did not arrive");
+      return -1;
+    }
     if (h.stop && !h.p_pending) break;
+  }
+  if (pairs && ((long long)(h.n - n_begin + 1) * (c.n_ppcg / 2)) % 2 != 0) {
+    // an odd number of fused pairs ran: the results are in r2/sd2
+    const size_t n = (size_t)((32 - (c.H % 32)) % 32 + c.rows * c.S + 32) * sizeof(double);
+    if (!check_cuda(cudaMemcpyAsync(c.r.base, c.r2.base, n, cudaMemcpyDeviceToDevice, c.stream),
+                    "resident PPCG r copy back") ||
+        !check_cuda(cudaMemcpyAsync(c.sd.base, c.sd2.base, n, cudaMemcpyDeviceToDevice,
+                                    c.stream),
+                    "resident PPCG sd copy back"))
+      return -1;
   }
   *rro_out = h.rro;
   *error_out = h.error;

@@ -62,6 +62,7 @@ struct MixChunk {
   unsigned int* counter = nullptr;
   cudaGraphExec_t graph = nullptr;
   int graph_batch = 0;
+  int graph_epoch = 0;  // the chunk's field_epoch at capture
 };
 
 static MixChunk g_mix;
@@ -722,10 +723,15 @@ static bool mixed_solve_t(Chunk& c, double tol, double inner_tol, int max_outer,
     k_mix_convert<<<grid, block, 0, c.stream>>>(d, g.dev);
     count_launch("mixed_convert");
   }
+  if (g.graph && g.graph_epoch != c.field_epoch) {
+    cudaGraphExecDestroy(g.graph);  // the chunk's r/sd buffers have traded places
+    g.graph = nullptr;
+  }
   if (!g.graph) {
     g.graph = mix_capture(c, [&]() { enqueue_inner<TH>(c, batch); });
     if (!g.graph) return false;
     g.graph_batch = batch;
+    g.graph_epoch = c.field_epoch;
   }
   double res[2];
   auto outer_residual = [&](double* out) -> bool {

@@ -84,7 +84,8 @@ def test_ppcg_log_reports_the_switch_in_the_reference_layout(tmp_path):
                     % (e14, e14, e14), eig[0]), repr(eig[0])
     tot = [ln for ln in text if ln.startswith("PPCG Iteration count")]
     for ln, s in zip(tot, steps):
-        m = re.match(r"^PPCG Iteration count([ \d]{8}) \(Total([ \d]{8})\)$", ln)
+        # FORMAT 103: 'PPCG Iteration count', i8, ' (Total ', i8, ')'
+        m = re.match(r"^PPCG Iteration count([ \d]{8}) \(Total ([ \d]{8})\)$", ln)
         assert m, repr(ln)
         assert int(m.group(1)) == s.inner_iterations
 
