@@ -72,6 +72,9 @@ ARITHMETIC = "chain"  # set from --arithmetic in main()
 # instead of 1 for z (5.5 when fused).  These kernels are bound by GB300's
 # FP64 pipe, not by HBM.
 FP64_PER_CELL = {
+    # two inner steps of update_r + calc_sd (6 + 2.5 each in the fused forms)
+    ("tea_leaf_ppcg_solve_inner_pair", "jac_block", "chain"): 17,
+    ("tea_leaf_ppcg_solve_inner_pair", "jac_block", "fused"): 17,
     ("tea_leaf_ppcg_solve_update_r", "jac_block", "chain"): 6,
     ("tea_leaf_ppcg_solve_update_r", "jac_block", "fused"): 6,
     ("tea_leaf_ppcg_solve_update_r", "jac_block", "exact"): 9,
@@ -241,10 +244,14 @@ def run_ours(args, dist):
     from tealeaf_opencl_gb300 import lib
 
     L = lib.load()
+    L.tea_gb300_set_inner_pairs(args.inner_pairs)
     name = args.workload
     cells = WORKLOADS[name][0]
     ncell = cells * cells
     kernel, bytes_per_cell = WORKLOADS[name][7], WORKLOADS[name][8]
+    if args.inner_pairs and WORKLOADS[name][1] == "ppcg" and WORKLOADS[name][2] == "jac_block":
+        # two inner steps per launch: reads u r sd Kx Ky diag cp bfp, writes u r sd
+        kernel, bytes_per_cell = "tea_leaf_ppcg_solve_inner_pair", 88
     steps_total = args.warmup + args.steps
     deck = deck_for(name, steps_total)
 
@@ -370,6 +377,7 @@ KERNEL_BYTES = {
     "tea_leaf_cg_solve_calc_p": 24,       # r z p, w p
     "tea_leaf_calc_2norm": 16,
     "tea_leaf_ppcg_solve_update_r": 56,   # r u r Kx Ky sd, w u r
+    "tea_leaf_ppcg_solve_inner_pair": 88,  # two steps: r u r sd Kx Ky diag cp bfp, w u r sd
     "tea_leaf_ppcg_solve_calc_sd": {"jac_diag": 32, "jac_block": 56, "none": 24},
     "tea_leaf_cheby_solve_calc_p": {"jac_diag": 80, "jac_block": 96, "none": 72},
     "tea_leaf_cheby_solve_calc_u": 24,
@@ -395,6 +403,7 @@ def run_kernels(args):
     import ctypes
     from tealeaf_opencl_gb300 import decks, lib
     L = lib.load()
+    L.tea_gb300_set_inner_pairs(args.inner_pairs)
     name = args.workload
     cells, solver, prec, halo = WORKLOADS[name][:4]
     ch = lib.Chunk(cells, cells, halo, "ppcg", prec)
@@ -786,6 +795,9 @@ def main():
     ap.add_argument("--cpu-cap-after-switch", type=int, default=9,
                     help="PPCG/Chebyshev workloads: iterations per CPU sample step "
                          "from the switch from CG on")
+    ap.add_argument("--inner-pairs", type=int, default=0, choices=[0, 1],
+                    help="PPCG inner steps two at a time in one TMA-fed pass (1) or one "
+                         "update_r + calc_sd launch pair per step (0, the faster on GB300)")
     ap.add_argument("--no-mixed", action="store_true",
                     help="leave out the mixed-precision comparison of the default line")
     ap.add_argument("--cap", type=int, default=0,

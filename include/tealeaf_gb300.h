@@ -217,6 +217,15 @@ int tea_gb300_set_arithmetic(int form);
  * Returns 0, or -1 for another value. */
 int tea_gb300_set_resident_mode(int mode);
 int tea_gb300_get_arithmetic(void);
+/* With the block-Jacobi preconditioner, PPCG inner steps can run two at a
+ * time in one pass whose inputs are staged in shared memory by TMA (1), or
+ * as one update_r + calc_sd pair of launches per step (0, default: on GB300
+ * the pair of launches measured faster, 648 against 864 us per two steps at
+ * 4096^2).  With 1, tea_leaf_ppcg_inner_kernel_ocl_ holds back a step that a
+ * next step may follow until that step (or any other call) arrives.
+ * Results are identical either way.  Applies to the current chunk and later
+ * ones.  Returns 0, or -1 for another value. */
+int tea_gb300_set_inner_pairs(int on);
 /* The persistent loop's grid barrier (mode 2 above): a block polls at most
  * spin_limit times (default 2^26, about 4 s) before it gives up, sets the
  * loop's error flag and returns; the call then fails with error 25.

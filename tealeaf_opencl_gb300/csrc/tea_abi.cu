@@ -259,6 +259,7 @@ struct Config {
   int resident_mode = 0;
   long long barrier_spin_limit = 1LL << 26;  // persistent loop's grid barrier
   int barrier_extra = 0;
+  int inner_pairs = 0;  // measured slower than the two kernels on GB300 (tea_ppcg_tb.cu)
 };
 static Config g_config;
 
@@ -336,6 +337,7 @@ static bool init_chunk(int x_max, int y_max, const Config& cfg) {
   c.resident_mode = cfg.resident_mode;
   c.barrier_spin_limit = cfg.barrier_spin_limit;
   c.barrier_extra = cfg.barrier_extra;
+  c.inner_pairs = cfg.inner_pairs;
   c.TH = reduction_rows(x_max, y_max);
   c.S = ((long long)(x_max + 2 * c.H + 1 + 31) / 32) * 32;
   c.rows = y_max + 2 * c.H + 1;
@@ -390,6 +392,7 @@ static bool need_chunk(const char* who) {
     return false;
   }
   flush_pending_inner(chunk());
+  chunk().abi_calls++;
   return true;
 }
 
@@ -679,8 +682,21 @@ extern "C" void tea_leaf_cg_calc_ur_kernel_ocl_(double* alpha, double* rrn) {
   const double a = *alpha;
   *rrn = NAN;
   if (!need_chunk("tea_leaf_cg_calc_ur_kernel_ocl_")) return;
-  arm_host_result(chunk());
-  launch_cg_calc_ur(chunk(), a);
+  Chunk& c = chunk();
+  arm_host_result(c);
+  // In a PPCG solve the next call is normally tea_leaf_ppcg_init_sd_kernel_ocl_
+  // (tea_solve.f90:247-249, :422-475), which forms sd = M^-1 r / theta from
+  // the r and z made here.  This pass forms it too, from its own z, into the
+  // spare sd buffer; init_sd then only makes that buffer current, provided no
+  // other call came in between (the current sd is untouched until then).
+  if (c.solver == SOLVER_PPCG && c.n_ppcg > 0 && ensure_alt_fields(c)) {
+    launch_cg_calc_ur_sd(c, a, c.ppcg_theta, c.sd2.f);
+    c.spec_sd_call = c.abi_calls;
+    c.spec_sd_theta = c.ppcg_theta;
+    c.spec_sd_arith = c.arith;
+  } else {
+    launch_cg_calc_ur(c, a);
+  }
   fetch(1, rrn);
 }
 
@@ -735,6 +751,14 @@ extern "C" void tea_leaf_ppcg_init_ocl_(const double* ch_alphas,
 extern "C" void tea_leaf_ppcg_init_sd_kernel_ocl_(void) {
   if (!need_chunk("tea_leaf_ppcg_init_sd_kernel_ocl_")) return;
   Chunk& c = chunk();
+  // the sd the last calc_ur formed, if this call directly follows it
+  if (c.spec_sd_call >= 0 && c.abi_calls == c.spec_sd_call + 1 &&
+      c.spec_sd_theta == c.ppcg_theta && c.spec_sd_arith == c.arith) {
+    c.spec_sd_call = -1;
+    std::swap(c.sd, c.sd2);
+    c.field_epoch++;
+    return;
+  }
   launch_ppcg_init_sd(c, c.ppcg_theta);
 }
 
@@ -882,6 +906,16 @@ extern "C" int tea_gb300_set_resident_mode(int mode) {
   }
   g_config.resident_mode = mode;
   chunk().resident_mode = mode;
+  return 0;
+}
+
+extern "C" int tea_gb300_set_inner_pairs(int on) {
+  if (on != 0 && on != 1) {
+    fail(3, "tea_gb300_set_inner_pairs: %d is not 0 or 1", on);
+    return -1;
+  }
+  if (chunk().ready) flush_pending_inner(chunk());
+  g_config.inner_pairs = chunk().inner_pairs = on;
   return 0;
 }
 

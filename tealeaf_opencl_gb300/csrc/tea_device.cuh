@@ -199,19 +199,20 @@ __device__ __forceinline__ double bwd(double dp, double cp, double z) {
 // EMU the multiplies by bfp run on the integer pipes (same bits).
 // The strip solve on values: bfp, Ky and cp of the strip's rows 0..3 (Ky of
 // row 0 and cp of row 3 unused), diag of row 0 (exact form only); entries of
-// rows at or past `upper` are not read.
-template <int F, bool EMU = false>
+// rows at or past `upper` are not read.  FULL: a whole strip (upper == 4),
+// without the row tests.
+template <int F, bool EMU = false, bool FULL = false>
 __device__ __forceinline__ void strip_solve_v(int upper, const double rl[4],
                                               const double bfp[4], const double ky[4],
                                               const double cp[4], double diag0,
                                               double zl[4]) {
   double dp0, dp1 = 0.0, dp2 = 0.0, dp3 = 0.0;
   dp0 = F ? mul_e<EMU>(rl[0], bfp[0]) : emu_ddiv_var(rl[0], diag0);
-  if (upper > 1) dp1 = fwd<F, EMU>(rl[1], ky[1], dp0, bfp[1]);
-  if (upper > 2) dp2 = fwd<F, EMU>(rl[2], ky[2], dp1, bfp[2]);
-  if (upper > 3) dp3 = fwd<F, EMU>(rl[3], ky[3], dp2, bfp[3]);
+  if (FULL || upper > 1) dp1 = fwd<F, EMU>(rl[1], ky[1], dp0, bfp[1]);
+  if (FULL || upper > 2) dp2 = fwd<F, EMU>(rl[2], ky[2], dp1, bfp[2]);
+  if (FULL || upper > 3) dp3 = fwd<F, EMU>(rl[3], ky[3], dp2, bfp[3]);
   double z0, z1 = 0.0, z2 = 0.0, z3 = 0.0;
-  if (upper == 4) {
+  if (FULL || upper == 4) {
     z3 = dp3;
     z2 = bwd<F>(dp2, cp[2], z3);
     z1 = bwd<F>(dp1, cp[1], z2);

@@ -130,8 +130,15 @@ struct Chunk {
   // (tea_ppcg_tb.cu), which writes r and sd to the pair it does not read;
   // allocated on first use, with the halos of the live pair
   Field r2, sd2;
+  int inner_pairs = 0;      // run PPCG inner steps in fused pairs where they apply
   int field_epoch = 0;      // bumped whenever r/sd and r2/sd2 trade places
   int pending_inner = -1;   // a per-call inner step (0-based) not launched yet
+  // PPCG's sd formed ahead by calc_ur into sd2 (tea_abi.cu): valid for the
+  // init_sd call that directly follows that calc_ur
+  long long abi_calls = 0;       // entry-point calls on this chunk
+  long long spec_sd_call = -1;   // abi_calls of that calc_ur, or -1
+  double spec_sd_theta = 0.0;
+  int spec_sd_arith = -1;
   int solver_checks = 0;               // next resident loop: stop on a breakdown
   // grid barrier of the persistent loop: polls before it gives up, and the
   // arrivals it waits for beyond the grid (nonzero only to test the time-out)
@@ -184,6 +191,8 @@ void launch_block_init(Chunk& c);
 void launch_cg_init_p(Chunk& c);
 void launch_cg_calc_w(Chunk& c);
 void launch_cg_calc_ur(Chunk& c, double alpha);
+// calc_ur and, from its z, PPCG's sd = M^-1 r / theta into sd_out
+void launch_cg_calc_ur_sd(Chunk& c, double alpha, double theta, double* sd_out);
 void launch_cg_calc_p(Chunk& c, double beta);
 void launch_cheby_init_p(Chunk& c, double theta);
 void launch_cheby_calc_p(Chunk& c, double alpha, double beta);

@@ -461,6 +461,17 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+// tea_leaf_cg_solve_calc_ur with its r.z, and PPCG's init_sd
+// (tea_leaf_ppcg_cl.cl:4-60) from the z it forms, into d.sd (the spare
+// buffer, so the current sd stays as it is until init_sd is called).
+template <int TH, int F>
+__global__ void __launch_bounds__(kBlock)
+    k_cg_calc_ur_sd(Dev d, Red red, double alpha, DivConst theta) {
+  tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    cg_ur_tile<TH, F, 1, false, true>(d, x, y0, xin, acc, alpha, theta);
+  });
+}
+
 // tea_leaf_cg_solve_calc_p, tea_leaf_cg_cl.cl:141-160.  In the
 // device-resident loop it runs once per calc_ur that ran, with that
 // iteration's beta.
@@ -963,6 +974,13 @@ void launch_cg_calc_w(Chunk& c) {
 void launch_cg_calc_ur(Chunk& c, double alpha) {
   TH_DISPATCH(c, "tea_leaf_cg_solve_calc_ur", k_cg_calc_ur, c.dev(), c.red(),
               alpha, (ResState*)nullptr);
+}
+
+void launch_cg_calc_ur_sd(Chunk& c, double alpha, double theta, double* sd_out) {
+  Dev d = c.dev();
+  d.sd = sd_out;
+  TH_DISPATCH(c, "tea_leaf_cg_solve_calc_ur", k_cg_calc_ur_sd, d, c.red(), alpha,
+              div_const(theta));
 }
 
 void launch_cg_calc_p(Chunk& c, double beta) {

@@ -156,47 +156,48 @@ __global__ void __launch_bounds__(TbShape<NWA>::kThreads)
         const double* Lp = slot_of(t + 2);  // strip a+1
         auto fld = [&](const double* L, int f, int i, int c) { return L[f * T::kFb + i * T::kWt + c]; };
         const int x = x0 - 1 + lane;
-        const bool xin = x >= 0 && x < g.x_max;
-        const bool strip_in = a >= 0 && a < g.ny;
+        const bool xs_in = x >= 0 && x < g.x_max && a >= 0 && a < g.ny;
+        // Every row is computed (shared memory holds finite halo or fill
+        // values everywhere) and the results outside the interior are
+        // discarded by selection: no branch separates the four rows, so
+        // their independent chains interleave.
         double rl[4], ul[4], sc[4];
+        bool in[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-          const bool in = xin && strip_in && 4 * a + i < g.y_max;
+          in[i] = xs_in && 4 * a + i < g.y_max;
           sc[i] = fld(L0, TB_SD, i, ci);
-          rl[i] = 0.0;
-          ul[i] = 0.0;
-          if (in) {
-            const double xn = i < 3 ? fld(L0, TB_SD, i + 1, ci) : fld(Lp, TB_SD, 0, ci);
-            const double xs = i > 0 ? fld(L0, TB_SD, i - 1, ci) : fld(Lm, TB_SD, 3, ci);
-            const double kyn = i < 3 ? fld(L0, TB_KY, i + 1, ci) : fld(Lp, TB_KY, 0, ci);
-            rl[i] = bms_v<F>(fld(L0, TB_R, i, ci), fld(L0, TB_DIAG, i, ci), kyn,
-                             fld(L0, TB_KY, i, ci), fld(L0, TB_KX, i, ci + 1),
-                             fld(L0, TB_KX, i, ci), sc[i], xn, xs, fld(L0, TB_SD, i, ci + 1),
-                             fld(L0, TB_SD, i, ci - 1));
-            ul[i] = fld(L0, TB_U, i, ci) + sc[i];
-          }
+          const double xn = i < 3 ? fld(L0, TB_SD, i + 1, ci) : fld(Lp, TB_SD, 0, ci);
+          const double xs = i > 0 ? fld(L0, TB_SD, i - 1, ci) : fld(Lm, TB_SD, 3, ci);
+          const double kyn = i < 3 ? fld(L0, TB_KY, i + 1, ci) : fld(Lp, TB_KY, 0, ci);
+          const double rv = bms_v<F>(fld(L0, TB_R, i, ci), fld(L0, TB_DIAG, i, ci), kyn,
+                                     fld(L0, TB_KY, i, ci), fld(L0, TB_KX, i, ci + 1),
+                                     fld(L0, TB_KX, i, ci), sc[i], xn, xs,
+                                     fld(L0, TB_SD, i, ci + 1), fld(L0, TB_SD, i, ci - 1));
+          rl[i] = in[i] ? rv : 0.0;
+          ul[i] = fld(L0, TB_U, i, ci) + sc[i];
         }
-        double zl[4] = {0.0, 0.0, 0.0, 0.0};
-        if (xin && strip_in) {
-          double bfp[4], ky[4], cp[4];
+        double zl[4], bfp[4], ky[4], cp[4];
 #pragma unroll
-          for (int i = 0; i < 4; i++) {
-            bfp[i] = fld(L0, TB_BFP, i, ci);
-            ky[i] = fld(L0, TB_KY, i, ci);
-            cp[i] = fld(L0, TB_CP, i, ci);
-          }
-          strip_solve_v<F, true>(rows_of(4 * a), rl, bfp, ky, cp, fld(L0, TB_DIAG, 0, ci), zl);
+        for (int i = 0; i < 4; i++) {
+          bfp[i] = fld(L0, TB_BFP, i, ci);
+          ky[i] = fld(L0, TB_KY, i, ci);
+          cp[i] = fld(L0, TB_CP, i, ci);
         }
+        const int upper = xs_in ? rows_of(4 * a) : 4;
+        if (upper == 4)
+          strip_solve_v<F, true, true>(4, rl, bfp, ky, cp, fld(L0, TB_DIAG, 0, ci), zl);
+        else
+          strip_solve_v<F, true>(upper, rl, bfp, ky, cp, fld(L0, TB_DIAG, 0, ci), zl);
         double* s1 = sd1 + ((a + 4) & 3) * T::kSd1;
         double* rr = r1 + ((a + 3) % 3) * T::kRu;
         double* uu = u1 + ((a + 3) % 3) * T::kRu;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-          const bool in = xin && strip_in && 4 * a + i < g.y_max;
+          const double sn = F ? __fma_rn(g.a0, sc[i], emu_dmul(g.b0, zl[i]))
+                              : g.a0 * sc[i] + emu_dmul(g.b0, zl[i]);
           // outside the interior sd keeps its stored (halo) value
-          s1[i * T::kWt + ci] = in ? (F ? __fma_rn(g.a0, sc[i], emu_dmul(g.b0, zl[i]))
-                                        : g.a0 * sc[i] + emu_dmul(g.b0, zl[i]))
-                                   : sc[i];
+          s1[i * T::kWt + ci] = in[i] ? sn : sc[i];
           rr[i * T::kLanes + lane] = rl[i];
           uu[i * T::kLanes + lane] = ul[i];
         }
@@ -212,43 +213,45 @@ __global__ void __launch_bounds__(TbShape<NWA>::kThreads)
         const double* rr = r1 + ((b + 3) % 3) * T::kRu;
         const double* uu = u1 + ((b + 3) % 3) * T::kRu;
         const int x = x0 - 1 + lane;
-        if (x >= x0 && x < x1 && x < g.x_max) {
-          double rl[4], sc[4], uv[4];
+        const bool own = x >= x0 && x < x1 && x < g.x_max;
+        // as in step k: every row and lane computes, the stores select
+        double rl[4], sc[4], uv[4];
+        bool in[4];
 #pragma unroll
-          for (int i = 0; i < 4; i++) {
-            const bool in = 4 * b + i < g.y_max;
-            sc[i] = Sc[i * T::kWt + ci];
-            rl[i] = 0.0;
-            uv[i] = 0.0;
-            if (in) {
-              const double xn = i < 3 ? Sc[(i + 1) * T::kWt + ci] : Sp[ci];
-              const double xs = i > 0 ? Sc[(i - 1) * T::kWt + ci] : Sm[3 * T::kWt + ci];
-              const double kyn = i < 3 ? fld(L0, TB_KY, i + 1, ci) : fld(Lp, TB_KY, 0, ci);
-              rl[i] = bms_v<F>(rr[i * T::kLanes + lane], fld(L0, TB_DIAG, i, ci), kyn,
-                               fld(L0, TB_KY, i, ci), fld(L0, TB_KX, i, ci + 1),
-                               fld(L0, TB_KX, i, ci), sc[i], xn, xs, Sc[i * T::kWt + ci + 1],
-                               Sc[i * T::kWt + ci - 1]);
-              uv[i] = uu[i * T::kLanes + lane] + sc[i];
-            }
-          }
-          double bfp[4], ky[4], cp[4], zl[4];
+        for (int i = 0; i < 4; i++) {
+          in[i] = own && 4 * b + i < g.y_max;
+          sc[i] = Sc[i * T::kWt + ci];
+          const double xn = i < 3 ? Sc[(i + 1) * T::kWt + ci] : Sp[ci];
+          const double xs = i > 0 ? Sc[(i - 1) * T::kWt + ci] : Sm[3 * T::kWt + ci];
+          const double kyn = i < 3 ? fld(L0, TB_KY, i + 1, ci) : fld(Lp, TB_KY, 0, ci);
+          const double rv = bms_v<F>(rr[i * T::kLanes + lane], fld(L0, TB_DIAG, i, ci), kyn,
+                                     fld(L0, TB_KY, i, ci), fld(L0, TB_KX, i, ci + 1),
+                                     fld(L0, TB_KX, i, ci), sc[i], xn, xs,
+                                     Sc[i * T::kWt + ci + 1], Sc[i * T::kWt + ci - 1]);
+          rl[i] = in[i] ? rv : 0.0;
+          uv[i] = uu[i * T::kLanes + lane] + sc[i];
+        }
+        double bfp[4], ky[4], cp[4], zl[4];
 #pragma unroll
-          for (int i = 0; i < 4; i++) {
-            bfp[i] = fld(L0, TB_BFP, i, ci);
-            ky[i] = fld(L0, TB_KY, i, ci);
-            cp[i] = fld(L0, TB_CP, i, ci);
-          }
-          strip_solve_v<F, true>(rows_of(4 * b), rl, bfp, ky, cp, fld(L0, TB_DIAG, 0, ci), zl);
+        for (int i = 0; i < 4; i++) {
+          bfp[i] = fld(L0, TB_BFP, i, ci);
+          ky[i] = fld(L0, TB_KY, i, ci);
+          cp[i] = fld(L0, TB_CP, i, ci);
+        }
+        const int upper = rows_of(4 * b);
+        if (upper == 4)
+          strip_solve_v<F, true, true>(4, rl, bfp, ky, cp, fld(L0, TB_DIAG, 0, ci), zl);
+        else
+          strip_solve_v<F, true>(upper, rl, bfp, ky, cp, fld(L0, TB_DIAG, 0, ci), zl);
 #pragma unroll
-          for (int i = 0; i < 4; i++) {
-            const int y = 4 * b + i;
-            if (y < g.y_max) {
-              const long long c = (long long)(y + g.H) * g.S + (x + g.H);
-              g.u[c] = uv[i];
-              g.r_out[c] = rl[i];
-              g.sd_out[c] = F ? __fma_rn(g.a1, sc[i], emu_dmul(g.b1, zl[i]))
+        for (int i = 0; i < 4; i++) {
+          const double sn = F ? __fma_rn(g.a1, sc[i], emu_dmul(g.b1, zl[i]))
                               : g.a1 * sc[i] + emu_dmul(g.b1, zl[i]);
-            }
+          if (in[i]) {
+            const long long c = (long long)(4 * b + i + g.H) * g.S + (x + g.H);
+            g.u[c] = uv[i];
+            g.r_out[c] = rl[i];
+            g.sd_out[c] = sn;
           }
         }
       }
@@ -344,7 +347,8 @@ static TbPlan tb_plan(const Chunk& c, int blocks_per_sm) {
 // The fused pair covers the block-Jacobi preconditioner on grids whose row
 // stride holds a whole copy box (kWt columns); others keep the two kernels.
 bool tb_applicable(const Chunk& c) {
-  return c.prec == PREC_JAC_BLOCK && c.S >= TbShape<kTbNwa>::kWt && c.y_max >= 1;
+  return c.inner_pairs && c.prec == PREC_JAC_BLOCK && c.S >= TbShape<kTbNwa>::kWt &&
+         c.y_max >= 1;
 }
 
 // The launcher state of the current chunk: a tensor map per field buffer

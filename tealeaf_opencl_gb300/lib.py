@@ -36,7 +36,7 @@ REFERENCE_SYMBOLS = [
 ]
 EXTRA_SYMBOLS = [
     "tea_gb300_configure", "tea_gb300_set_arithmetic", "tea_gb300_get_arithmetic",
-    "tea_gb300_set_resident_mode", "tea_gb300_set_barrier_limits",
+    "tea_gb300_set_resident_mode", "tea_gb300_set_barrier_limits", "tea_gb300_set_inner_pairs",
     "tea_gb300_set_abort_on_error", "tea_gb300_last_error",
     "tea_gb300_finalise", "tea_gb300_read_field", "tea_gb300_write_field",
     "tea_gb300_read_field_padded", "tea_gb300_write_field_padded",
@@ -180,6 +180,7 @@ def load(build=True):
         "tea_gb300_get_arithmetic": (i, []),
         "tea_gb300_set_resident_mode": (i, [i]),
         "tea_gb300_set_barrier_limits": (i, [C.c_longlong, i]),
+        "tea_gb300_set_inner_pairs": (i, [i]),
         "tea_gb300_last_error": (i, [C.c_char_p, i]),
         "tea_gb300_finalise": (v, []),
         "tea_gb300_read_field": (i, [i, PD]),

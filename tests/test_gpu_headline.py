@@ -72,3 +72,17 @@ def test_headline_ppcg_per_call_matches_pin():
     """The per-call C ABI (bench.py's e2e path) gives the pinned bits too."""
     p = pin("ppcg4096", "chain")
     assert_matches_pin(run(p, lib.DRIVER_PER_CALL), p)
+
+
+@pytest.mark.parametrize("form", ["exact", "chain"])
+def test_headline_ppcg_with_fused_inner_pairs_matches_pin(form):
+    """The TMA-fed pair of inner steps (tea_gb300_set_inner_pairs(1)) gives
+    the pinned bits at the benchmark's own size, resident and per call."""
+    L = lib.load()
+    p = pin("ppcg4096", form)
+    L.tea_gb300_set_inner_pairs(1)
+    try:
+        assert_matches_pin(run(p, lib.DRIVER_RESIDENT), p)
+        assert_matches_pin(run(p, lib.DRIVER_PER_CALL), p)
+    finally:
+        L.tea_gb300_set_inner_pairs(0)

@@ -22,6 +22,16 @@ pytestmark = pytest.mark.gpu
 PAIR = b"tea_leaf_ppcg_solve_inner_pair"
 
 
+@pytest.fixture(autouse=True)
+def pairs_on():
+    """The fused pairs are off by default (slower on GB300); these tests
+    switch them on."""
+    L = lib.load()
+    assert L.tea_gb300_set_inner_pairs(1) == 0
+    yield
+    L.tea_gb300_set_inner_pairs(0)
+
+
 def run_counting_pairs(deck, mode):
     L = lib.load()
     L.tea_gb300_kernel_timer_select(PAIR)
@@ -84,4 +94,41 @@ def test_held_step_is_launched_before_a_field_read():
         ch.ppcg_inner(4)  # paired with 3
         recs[-1] += (ch.read("r"), ch.read("sd"), ch.read("u"))
     for g, o in zip(*recs):
+        assert (g.view("u8") == o.view("u8")).all()
+
+
+@pytest.mark.parametrize("prec", [3, 2, 1])
+def test_calc_ur_forms_sd_ahead_without_showing_it(prec):
+    """In a PPCG chunk tea_leaf_cg_calc_ur_kernel_ocl_ also forms init_sd's
+    sd into a spare buffer; init_sd uses it only when it directly follows.
+    A read in between sees the old sd, and both orders give the oracle's
+    fields."""
+    from tests import scenarios
+    x, y, H = 130, 97, 2
+    out = []
+    for backend in ("gpu", "oracle"):
+        mk = lib.Chunk if backend == "gpu" else oracle.Chunk
+        ch = mk(x, y, H, 4, prec)
+        scenarios.setup(ch, x, y, halo=H)
+        ch.common_init(1, 0.004)
+        ch.calc_residual()
+        rro = ch.cg_init()
+        a, b, theta = scenarios.ch_coefs(0.9, 40.0, 4)
+        ch.ppcg_init(a, b, theta)
+        rec = []
+        pw = ch.cg_calc_w()
+        rrn = ch.cg_calc_ur(rro / pw)
+        rec.append(ch.read("sd"))  # between calc_ur and init_sd
+        ch.ppcg_init_sd()
+        rec.append(ch.read("sd"))
+        for s in range(1, 5):
+            ch.ppcg_inner(s)
+        rro = ch.calc_2norm(2)
+        ch.cg_calc_p(rro / rrn)
+        pw = ch.cg_calc_w()
+        ch.cg_calc_ur(rro / pw)
+        ch.ppcg_init_sd()  # directly after calc_ur
+        rec += [ch.read("sd"), ch.read("r"), ch.read("u"), ch.read("z")]
+        out.append(rec)
+    for g, o in zip(*out):
         assert (g.view("u8") == o.view("u8")).all()
