@@ -1,7 +1,11 @@
 """Regenerates the golden fixtures in tests/golden/ from the reference tree.
 
-Run in a container that has the reference mounted (its path is the first
-argument, default /root/reference).  It copies the reference's input decks,
+Run where the reference tree is available; its location is the one
+required argument:
+
+    python tests/golden/make_golden.py <path of the reference tree>
+
+It copies the reference's input decks,
 writes the built-in test-problem-1 deck that initialise.f90:67-92 generates
 when tea.in is missing, and extracts the known-answer temperatures of
 field_summary.f90:88-106.  Nothing at test time reads the reference.
@@ -11,7 +15,7 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = None  # the reference tree, from the command line
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 DECKS = {2: "tea_bm_short.in", 3: "tea_bm16_short.in", 4: "tea_bm.in",
@@ -54,4 +58,7 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) != 2 or not os.path.isdir(sys.argv[1]):
+        sys.exit("usage: make_golden.py <path of the reference tree>")
+    REF = sys.argv[1]
     main()
