@@ -450,6 +450,10 @@ typedef struct {
   int blocks_per_sm;         /* resident blocks per SM of each kernel (1..8) */
   int graph_iterations;      /* CG iterations per graph replay (1..64) */
   int supertiles_per_unit;   /* 256-column supertiles per work unit (1..64) */
+  int persistent;            /* 0: three kernels per CG iteration, replayed from
+                                a CUDA graph; 1: one persistent (cooperative)
+                                kernel per replay running its iterations with
+                                grid barriers between the phases */
 } tea_gb300_batch_launch;
 
 /* Creates a batch of n problems; problem i has x_cells[i] x y_cells[i]
@@ -479,9 +483,10 @@ int tea_gb300_batch_read_field(int i, int field, double* out);
 /* Sets / reads the launch geometry. */
 int tea_gb300_batch_set_launch(const tea_gb300_batch_launch* launch);
 int tea_gb300_batch_get_launch(tea_gb300_batch_launch* launch);
-/* Times one CG iteration phase per candidate geometry on the batch's
- * current state (restored afterwards) and keeps the fastest; best gets the
- * choice.  The fields and every later result are unchanged by the search. */
+/* Times CG iterations per candidate geometry (three-kernel or persistent
+ * launch, blocks per SM, supertiles per unit) on the batch's current state
+ * (restored afterwards) and keeps the fastest; best gets the choice.  The
+ * fields and every later result are unchanged by the search. */
 int tea_gb300_batch_autotune(tea_gb300_batch_launch* best);
 /* Releases the batch. */
 void tea_gb300_batch_free(void);

@@ -140,15 +140,25 @@ __device__ __forceinline__ bool unit_done(unsigned int* counter, int units,
   return *is_last != 0u;
 }
 
+// A double of the loop state written by another block of the same
+// (persistent) launch is read through L2 (CG); plain otherwise.
+template <bool CG>
+__device__ __forceinline__ double st_load(const double* p) {
+  return CG ? __ldcg(p) : *p;
+}
+
+// The three phases of one CG iteration over the block's work units.  The
+// separate kernels below run one phase each; k_b_iterations runs them in
+// turn with grid barriers between them (CG = true: fields and loop state
+// written by other blocks in an earlier phase are read through L2).
+
 // w = A p and p.w of every active problem (tea_leaf_cg_cl.cl:45-69); the
 // finishing block stores pw in the problem's loop state.
-template <int F>
-__global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
-    k_b_calc_w(const Dev* __restrict__ devs, const Red* __restrict__ reds,
-               ResState* st, WorkList wl) {
-  __shared__ double sh[32];
-  __shared__ unsigned int is_last;
-  const int U = wl.counts[0], np = wl.counts[1];
+template <int F, bool CG>
+__device__ __forceinline__ void phase_w(const Dev* __restrict__ devs,
+                                        const Red* __restrict__ reds, ResState* st,
+                                        const WorkList& wl, int U, int np, double* sh,
+                                        unsigned int* is_last) {
   for (int u = blockIdx.x; u < U; u += gridDim.x) {
     const int j = find_problem(wl, np, u);
     const int i = wl.plist[j];
@@ -158,11 +168,11 @@ __global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
     const int s0 = (u - wl.ustart[j]) * wl.G, s1 = min(s0 + wl.G, d.ns);
     unit_partials(d, red, s0, s1, sh, [&](int x, int y0, bool xin, double* a) {
       if (d.th == 16)
-        cg_w_tile<16, F>(d, x, y0, xin, a);
+        cg_w_tile<16, F, CG>(d, x, y0, xin, a);
       else
-        cg_w_tile<4, F>(d, x, y0, xin, a);
+        cg_w_tile<4, F, CG>(d, x, y0, xin, a);
     });
-    if (unit_done(red.counter, units_of(d.ns, wl.G), &is_last)) {
+    if (unit_done(red.counter, units_of(d.ns, wl.G), is_last)) {
       block_final_sum<1>(red.partials, red.stride, d.ns, red.result, sh);
       if (threadIdx.x == 0) {
         st[i].pw = red.result[0];
@@ -175,28 +185,26 @@ __global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
 
 // u, r, z updates and r.z (tea_leaf_cg_cl.cl:73-137) with alpha = rro/pw;
 // the finishing block takes the problem's scalar step and exit test.
-template <int F>
-__global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
-    k_b_calc_ur(const Dev* __restrict__ devs, const Red* __restrict__ reds,
-                ResState* st, WorkList wl) {
-  __shared__ double sh[32];
-  __shared__ unsigned int is_last;
-  const int U = wl.counts[0], np = wl.counts[1];
+template <int F, bool CG>
+__device__ __forceinline__ void phase_ur(const Dev* __restrict__ devs,
+                                         const Red* __restrict__ reds, ResState* st,
+                                         const WorkList& wl, int U, int np, double* sh,
+                                         unsigned int* is_last) {
   for (int u = blockIdx.x; u < U; u += gridDim.x) {
     const int j = find_problem(wl, np, u);
     const int i = wl.plist[j];
     if (*(volatile int*)&st[i].stop) continue;
     const Dev d = devs[i];
     const Red red = reds[i];
-    const double alpha = st[i].rro / st[i].pw;
+    const double alpha = st_load<CG>(&st[i].rro) / st_load<CG>(&st[i].pw);
     const int s0 = (u - wl.ustart[j]) * wl.G, s1 = min(s0 + wl.G, d.ns);
     unit_partials(d, red, s0, s1, sh, [&](int x, int y0, bool xin, double* a) {
       if (d.th == 16)
-        cg_ur_tile<16, F, 1>(d, x, y0, xin, a, alpha);
+        cg_ur_tile<16, F, 1, CG>(d, x, y0, xin, a, alpha);
       else
-        cg_ur_tile<4, F, 1>(d, x, y0, xin, a, alpha);
+        cg_ur_tile<4, F, 1, CG>(d, x, y0, xin, a, alpha);
     });
-    if (unit_done(red.counter, units_of(d.ns, wl.G), &is_last)) {
+    if (unit_done(red.counter, units_of(d.ns, wl.G), is_last)) {
       block_final_sum<1>(red.partials, red.stride, d.ns, red.result, sh);
       if (threadIdx.x == 0) {
         cg_scalar_step<1>(&st[i], alpha, red.result);
@@ -209,36 +217,86 @@ __global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
 
 // p = z + beta p (tea_leaf_cg_cl.cl:141-160) for every problem whose
 // calc_ur has just run, including the iteration on which it stopped.
-template <int F>
-__global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
-    k_b_calc_p(const Dev* __restrict__ devs, const Red* __restrict__ reds,
-               ResState* st, WorkList wl) {
-  __shared__ unsigned int is_last;
-  const int U = wl.counts[0], np = wl.counts[1];
+template <int F, bool CG>
+__device__ __forceinline__ void phase_p(const Dev* __restrict__ devs,
+                                        const Red* __restrict__ reds, ResState* st,
+                                        const WorkList& wl, int U, int np,
+                                        unsigned int* is_last) {
   for (int u = blockIdx.x; u < U; u += gridDim.x) {
     const int j = find_problem(wl, np, u);
     const int i = wl.plist[j];
     if (!*(volatile int*)&st[i].p_pending) continue;
     const Dev d = devs[i];
     const Red red = reds[i];
-    const double beta = st[i].beta;
+    const double beta = st_load<CG>(&st[i].beta);
     const int s0 = (u - wl.ustart[j]) * wl.G, s1 = min(s0 + wl.G, d.ns);
     for (int s = s0; s < s1; s++) {
       double acc[1];
       run_supertile<0>(d, s, acc, [&](int x, int y0, bool xin, double* a) {
         if (d.th == 16)
-          cg_p_tile<16, F>(d, x, y0, xin, beta);
+          cg_p_tile<16, F, CG>(d, x, y0, xin, beta);
         else
-          cg_p_tile<4, F>(d, x, y0, xin, beta);
+          cg_p_tile<4, F, CG>(d, x, y0, xin, beta);
       });
     }
-    if (unit_done(red.counter, units_of(d.ns, wl.G), &is_last)) {
+    if (unit_done(red.counter, units_of(d.ns, wl.G), is_last)) {
       if (threadIdx.x == 0) {
         st[i].p_pending = 0;
         __threadfence();
       }
       __syncthreads();
     }
+  }
+}
+
+template <int F>
+__global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
+    k_b_calc_w(const Dev* __restrict__ devs, const Red* __restrict__ reds,
+               ResState* st, WorkList wl) {
+  __shared__ double sh[32];
+  __shared__ unsigned int is_last;
+  phase_w<F, false>(devs, reds, st, wl, wl.counts[0], wl.counts[1], sh, &is_last);
+}
+
+template <int F>
+__global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
+    k_b_calc_ur(const Dev* __restrict__ devs, const Red* __restrict__ reds,
+                ResState* st, WorkList wl) {
+  __shared__ double sh[32];
+  __shared__ unsigned int is_last;
+  phase_ur<F, false>(devs, reds, st, wl, wl.counts[0], wl.counts[1], sh, &is_last);
+}
+
+template <int F>
+__global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
+    k_b_calc_p(const Dev* __restrict__ devs, const Red* __restrict__ reds,
+               ResState* st, WorkList wl) {
+  __shared__ unsigned int is_last;
+  phase_p<F, false>(devs, reds, st, wl, wl.counts[0], wl.counts[1], &is_last);
+}
+
+// `iters` CG iterations of every active problem in one cooperative launch:
+// the three phases above with grid barriers between them (all blocks are
+// resident).  The active list is fixed for the launch (problems that stop
+// are skipped, as in the separate kernels); bar[0..1] is the barrier,
+// bar[2] its error flag, set if a barrier times out, after which every
+// block returns.  Results are those of the separate kernels.
+template <int F>
+__global__ void __launch_bounds__(kBlock, kBatchMinBlocks)
+    k_b_iterations(const Dev* __restrict__ devs, const Red* __restrict__ reds,
+                   ResState* st, WorkList wl, int iters, unsigned int* bar,
+                   long long spin_limit) {
+  __shared__ double sh[32];
+  __shared__ unsigned int is_last;
+  int* err = (int*)(bar + 2);
+  const int U = wl.counts[0], np = wl.counts[1];
+  for (int it = 0; it < iters; it++) {
+    phase_w<F, true>(devs, reds, st, wl, U, np, sh, &is_last);
+    if (!grid_barrier(bar, err, spin_limit)) return;
+    phase_ur<F, true>(devs, reds, st, wl, U, np, sh, &is_last);
+    if (!grid_barrier(bar, err, spin_limit)) return;
+    phase_p<F, true>(devs, reds, st, wl, U, np, &is_last);
+    if (!grid_barrier(bar, err, spin_limit)) return;
   }
 }
 
@@ -388,7 +446,9 @@ struct Batch {
   int* plist_d = nullptr;       // active list (WorkList)
   int* ustart_d = nullptr;
   int* counts_d = nullptr;
-  int* counts_h = nullptr;      // pinned copy of counts_d after a replay
+  int* counts_h = nullptr;      // pinned copy of counts_d after a replay, and
+                                // [2] the persistent launch's barrier error flag
+  unsigned int* bar_d = nullptr;  // grid barrier of k_b_iterations [2] + error flag
   int* iters_d = nullptr;       // [iters_cap steps][n]
   int iters_cap = 0;
   std::vector<int> iters_h;     // [last_steps][n]
@@ -397,12 +457,13 @@ struct Batch {
   std::vector<int> order;       // problems, largest first
   std::vector<double> summary_h;
   bool summary_valid = false;
-  tea_gb300_batch_launch launch{0, 16, 1};
+  tea_gb300_batch_launch launch{0, 16, 1, 0};
   int ustart_G = 0;             // G that ustart_all_d was built for
   int max_bps = 1;
   int occ[3][3] = {};  // [arithmetic form][w, ur, p]
+  int occ_persistent[3] = {};  // [arithmetic form] k_b_iterations
   cudaGraphExec_t iter_graph = nullptr;
-  int graph_bps = 0, graph_iters = 0, graph_G = 0;
+  int graph_bps = 0, graph_iters = 0, graph_G = 0, graph_persistent = 0;
 };
 
 Batch g_batch;
@@ -431,6 +492,7 @@ void release_batch() {
   cudaFree(b.plist_d);
   cudaFree(b.ustart_d);
   cudaFree(b.counts_d);
+  cudaFree(b.bar_d);
   cudaFree(b.iters_d);
   cudaFreeHost(b.results_h);
   cudaFreeHost(b.counts_h);
@@ -473,6 +535,9 @@ int set_occupancy(Batch& b) {
   b.occ[2][0] = occupancy((const void*)k_b_calc_w<2>);
   b.occ[2][1] = occupancy((const void*)k_b_calc_ur<2>);
   b.occ[2][2] = occupancy((const void*)k_b_calc_p<2>);
+  b.occ_persistent[0] = occupancy((const void*)k_b_iterations<0>);
+  b.occ_persistent[1] = occupancy((const void*)k_b_iterations<1>);
+  b.occ_persistent[2] = occupancy((const void*)k_b_iterations<2>);
   int m = 1;
   for (int f = 0; f < 3; f++)
     for (int k = 0; k < 3; k++) m = std::max(m, b.occ[f][k]);
@@ -580,7 +645,8 @@ extern "C" int tea_gb300_batch_create(int n, const int* x_cells, const int* y_ce
       !check_cuda(cudaMalloc(&b.plist_d, n * sizeof(int)), "cudaMalloc plist") ||
       !check_cuda(cudaMalloc(&b.ustart_d, (n + 1) * sizeof(int)), "cudaMalloc ustart") ||
       !check_cuda(cudaMalloc(&b.counts_d, 2 * sizeof(int)), "cudaMalloc counts") ||
-      !check_cuda(cudaMallocHost(&b.counts_h, 2 * sizeof(int)), "cudaMallocHost counts") ||
+      !check_cuda(cudaMallocHost(&b.counts_h, 3 * sizeof(int)), "cudaMallocHost counts") ||
+      !check_cuda(cudaMalloc(&b.bar_d, 3 * sizeof(unsigned int)), "cudaMalloc batch barrier") ||
       !check_cuda(cudaMalloc(&b.st_d, n * sizeof(ResState)), "cudaMalloc batch state")) {
     release_batch();
     return -1;
@@ -832,21 +898,57 @@ void enqueue_iteration(Batch& b, const WorkList& wl, int bps) {
   k_b_calc_p<F><<<grid(2), kBlock, 0, b.stream>>>(b.devs_d, b.reds_d, b.st_d, wl);
 }
 
+// All `iters` iterations as one cooperative launch of k_b_iterations: as
+// many blocks as are resident at once (bps per SM, capped by the kernel's
+// occupancy), the barrier words cleared first.
+template <int F>
+void enqueue_persistent(Batch& b, const WorkList& wl, int iters, int bps) {
+  const int grid = std::max(1, b.num_sms * std::min(bps, b.occ_persistent[F]));
+  cudaMemsetAsync(b.bar_d, 0, 3 * sizeof(unsigned int), b.stream);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kBlock);
+  cfg.stream = b.stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const long long spin_limit = 1LL << 26;
+  check_cuda(cudaLaunchKernelEx(&cfg, k_b_iterations<F>, (const Dev*)b.devs_d,
+                                (const Red*)b.reds_d, b.st_d, wl, iters, b.bar_d, spin_limit),
+             "batch persistent launch");
+}
+
 int enqueue_iterations(Batch& b, int iters, int bps, bool compact) {
   const WorkList wl = work_list(b);
-  for (int k = 0; k < iters; k++) {
+  int launched = 0;
+  if (b.launch.persistent) {
     if (b.arith == 2)
-      enqueue_iteration<2>(b, wl, bps);
+      enqueue_persistent<2>(b, wl, iters, bps);
     else if (b.arith == 1)
-      enqueue_iteration<1>(b, wl, bps);
+      enqueue_persistent<1>(b, wl, iters, bps);
     else
-      enqueue_iteration<0>(b, wl, bps);
+      enqueue_persistent<0>(b, wl, iters, bps);
+    launched = 1;
+  } else {
+    for (int k = 0; k < iters; k++) {
+      if (b.arith == 2)
+        enqueue_iteration<2>(b, wl, bps);
+      else if (b.arith == 1)
+        enqueue_iteration<1>(b, wl, bps);
+      else
+        enqueue_iteration<0>(b, wl, bps);
+    }
+    launched = 3 * iters;
   }
-  int launched = 3 * iters;
   if (compact) {
     k_b_compact<<<1, 1024, 0, b.stream>>>(b.devs_d, b.st_d, b.plist_d, b.ustart_d,
                                           b.counts_d, wl.G);
     cudaMemcpyAsync(b.counts_h, b.counts_d, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                    b.stream);
+    // the persistent launch's barrier error flag, for the host's check
+    cudaMemcpyAsync(b.counts_h + 2, b.bar_d + 2, sizeof(int), cudaMemcpyDeviceToHost,
                     b.stream);
     launched++;
   }
@@ -895,7 +997,8 @@ extern "C" int tea_gb300_batch_run(int steps, double dt, double eps, int max_ite
   const int bps = std::min(std::max(b.launch.blocks_per_sm, 1), b.max_bps);
   const int gi = b.launch.graph_iterations;
   if (b.iter_graph && (b.graph_bps != bps || b.graph_iters != gi ||
-                       b.graph_G != b.launch.supertiles_per_unit)) {
+                       b.graph_G != b.launch.supertiles_per_unit ||
+                       b.graph_persistent != b.launch.persistent)) {
     cudaGraphExecDestroy(b.iter_graph);
     b.iter_graph = nullptr;
   }
@@ -906,8 +1009,10 @@ extern "C" int tea_gb300_batch_run(int steps, double dt, double eps, int max_ite
     b.graph_bps = bps;
     b.graph_iters = gi;
     b.graph_G = b.launch.supertiles_per_unit;
+    b.graph_persistent = b.launch.persistent;
   }
-  per_replay = 3 * gi + 1;
+  per_replay = b.launch.persistent ? 2 : 3 * gi + 1;
+  b.counts_h[2] = 0;
   long long n0 = tea_gb300_kernel_launches();
   cudaGraphExec_t pro = capture(b, [&]() { enqueue_prologue(b, dt, eps, max_iters); });
   const long long pro_nodes = tea_gb300_kernel_launches() - n0;
@@ -946,6 +1051,11 @@ extern "C" int tea_gb300_batch_run(int steps, double dt, double eps, int max_ite
       if (launched < 2) continue;
       if (!check_cuda(cudaEventSynchronize(b.replay[(launched - 2) % 2]), "batch replay"))
         return done(-1);
+      if (((volatile int*)b.counts_h)[2] != 0) {
+        fail(57, "batch: a grid barrier of the persistent iterations timed out");
+        cudaStreamSynchronize(b.stream);
+        return done(-1);
+      }
       if (((volatile int*)b.counts_h)[1] == 0) break;
     }
     replays += launched;
@@ -1036,9 +1146,10 @@ extern "C" int tea_gb300_batch_set_launch(const tea_gb300_batch_launch* launch) 
   Batch& b = g_batch;
   if (!launch || launch->blocks_per_sm < 1 || launch->blocks_per_sm > b.max_bps ||
       launch->graph_iterations < 1 || launch->graph_iterations > 64 ||
-      launch->supertiles_per_unit < 1 || launch->supertiles_per_unit > 64) {
+      launch->supertiles_per_unit < 1 || launch->supertiles_per_unit > 64 ||
+      launch->persistent < 0 || launch->persistent > 1) {
     fail(56, "tea_gb300_batch_set_launch: blocks_per_sm must be 1..%d, "
-             "graph_iterations 1..64, supertiles_per_unit 1..64",
+             "graph_iterations 1..64, supertiles_per_unit 1..64, persistent 0 or 1",
          b.max_bps);
     return -1;
   }
@@ -1067,28 +1178,46 @@ extern "C" int tea_gb300_batch_autotune(tea_gb300_batch_launch* best) {
       return -1;
     }
     enqueue_prologue(b, 0.004, 0.0, 1 << 30);
-    for (int bps = 1; bps <= b.max_bps; bps++) {
-      enqueue_iterations(b, 1, bps, false);  // warm-up
-      float ms_min = 0.0f;
-      for (int rep = 0; rep < 2; rep++) {
-        cudaEventRecord(b.s0, b.stream);
-        enqueue_iterations(b, timed, bps, false);
-        cudaEventRecord(b.s1, b.stream);
-        float ms = 0.0f;
-        if (!check_cuda(cudaEventSynchronize(b.s1), "batch autotune") ||
-            !check_cuda(cudaEventElapsedTime(&ms, b.s0, b.s1), "batch autotune")) {
-          b.launch = keep;
-          return -1;
+    // three kernels per iteration, or one persistent launch per replay
+    for (int persistent = 0; persistent < 2; persistent++) {
+      b.launch.persistent = persistent;
+      const int top = persistent ? std::min(b.max_bps, b.occ_persistent[b.arith]) : b.max_bps;
+      for (int bps = 1; bps <= top; bps++) {
+        enqueue_iterations(b, 1, bps, false);  // warm-up
+        float ms_min = 0.0f;
+        for (int rep = 0; rep < 2; rep++) {
+          cudaEventRecord(b.s0, b.stream);
+          enqueue_iterations(b, timed, bps, false);
+          cudaEventRecord(b.s1, b.stream);
+          float ms = 0.0f;
+          if (!check_cuda(cudaEventSynchronize(b.s1), "batch autotune") ||
+              !check_cuda(cudaEventElapsedTime(&ms, b.s0, b.s1), "batch autotune")) {
+            b.launch = keep;
+            return -1;
+          }
+          count_launches(persistent ? 1 : 3 * timed);
+          if (rep == 0 || ms < ms_min) ms_min = ms;
         }
-        count_launches(3 * timed);
-        if (rep == 0 || ms < ms_min) ms_min = ms;
-      }
-      count_launches(3);
-      if (!have || ms_min < best_ms) {
-        have = true;
-        best_ms = ms_min;
-        choice.blocks_per_sm = bps;
-        choice.supertiles_per_unit = G;
+        count_launches(persistent ? 1 : 3);
+        if (persistent) {
+          // a launch whose barrier timed out returned early: never a candidate
+          unsigned int flag = 0;
+          if (!check_cuda(cudaMemcpy(&flag, b.bar_d + 2, sizeof(flag), cudaMemcpyDeviceToHost),
+                          "batch autotune barrier flag") ||
+              flag != 0) {
+            if (flag)
+              fail(57, "batch autotune: a grid barrier of the persistent iterations timed out");
+            b.launch = keep;
+            return -1;
+          }
+        }
+        if (!have || ms_min < best_ms) {
+          have = true;
+          best_ms = ms_min;
+          choice.blocks_per_sm = bps;
+          choice.supertiles_per_unit = G;
+          choice.persistent = persistent;
+        }
       }
     }
   }

@@ -105,7 +105,7 @@ class BatchStats(C.Structure):
 
 class BatchLaunch(C.Structure):
     _fields_ = [("blocks_per_sm", C.c_int), ("graph_iterations", C.c_int),
-                ("supertiles_per_unit", C.c_int)]
+                ("supertiles_per_unit", C.c_int), ("persistent", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -553,8 +553,10 @@ class Batch:
             check()
         return l.as_dict()
 
-    def set_launch(self, blocks_per_sm, graph_iterations=16, supertiles_per_unit=1):
-        l = BatchLaunch(int(blocks_per_sm), int(graph_iterations), int(supertiles_per_unit))
+    def set_launch(self, blocks_per_sm, graph_iterations=16, supertiles_per_unit=1,
+                   persistent=0):
+        l = BatchLaunch(int(blocks_per_sm), int(graph_iterations), int(supertiles_per_unit),
+                        int(persistent))
         if load().tea_gb300_batch_set_launch(C.byref(l)) != 0:
             check()
             raise TeaError("batch_set_launch failed")

@@ -97,16 +97,18 @@ def test_launch_geometry_and_autotune_do_not_change_results():
     b = make_batch(problems, fields, "jac_diag", "fused")
     try:
         base = None
-        geoms = [(1, 1, 1), (2, 5, 3), (b.launch()["blocks_per_sm"], 16, 8)]
-        for bps, gi, g in geoms:
+        # the last three: one persistent (cooperative) launch per replay
+        geoms = [(1, 1, 1, 0), (2, 5, 3, 0), (b.launch()["blocks_per_sm"], 16, 8, 0),
+                 (1, 1, 1, 1), (2, 7, 2, 1), (b.launch()["blocks_per_sm"], 16, 4, 1)]
+        for bps, gi, g, pers in geoms:
             for i, f in enumerate(fields):
                 b.set_fields(i, *f)
-            b.set_launch(bps, gi, g)
+            b.set_launch(bps, gi, g, pers)
             b.run(2, DT, EPS, 5000)
             got = [(b.iterations(i), bits(b.summary(i))) for i in range(len(problems))]
             if base is None:
                 base = got
-            assert got == base, (bps, gi, g)
+            assert got == base, (bps, gi, g, pers)
         for i, f in enumerate(fields):
             b.set_fields(i, *f)
         best = b.autotune()
