@@ -647,6 +647,8 @@ extern "C" int tea_gb300_batch_create(int n, const int* x_cells, const int* y_ce
       !check_cuda(cudaMalloc(&b.counts_d, 2 * sizeof(int)), "cudaMalloc counts") ||
       !check_cuda(cudaMallocHost(&b.counts_h, 3 * sizeof(int)), "cudaMallocHost counts") ||
       !check_cuda(cudaMalloc(&b.bar_d, 3 * sizeof(unsigned int)), "cudaMalloc batch barrier") ||
+      !check_cuda(cudaMemsetAsync(b.bar_d, 0, 3 * sizeof(unsigned int), b.stream),
+                  "cudaMemset batch barrier") ||
       !check_cuda(cudaMalloc(&b.st_d, n * sizeof(ResState)), "cudaMalloc batch state")) {
     release_batch();
     return -1;
@@ -948,8 +950,9 @@ int enqueue_iterations(Batch& b, int iters, int bps, bool compact) {
     cudaMemcpyAsync(b.counts_h, b.counts_d, 2 * sizeof(int), cudaMemcpyDeviceToHost,
                     b.stream);
     // the persistent launch's barrier error flag, for the host's check
-    cudaMemcpyAsync(b.counts_h + 2, b.bar_d + 2, sizeof(int), cudaMemcpyDeviceToHost,
-                    b.stream);
+    if (b.launch.persistent)
+      cudaMemcpyAsync(b.counts_h + 2, b.bar_d + 2, sizeof(int), cudaMemcpyDeviceToHost,
+                      b.stream);
     launched++;
   }
   check_cuda(cudaGetLastError(), "batch iterations");
