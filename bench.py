@@ -575,6 +575,12 @@ def run_batch(args):
     t0 = time.perf_counter()
     tuned = b.autotune()
     tune_s = time.perf_counter() - t0
+    if args.batch_launch != "auto":
+        # the tuned geometry with the launch mode forced
+        tuned["persistent"] = 1 if args.batch_launch == "persistent" else 0
+        b.set_launch(tuned["blocks_per_sm"], tuned["graph_iterations"],
+                     tuned["supertiles_per_unit"], tuned["persistent"])
+        tuned = b.launch()
     runs = []
     for rep in range(max(1, args.reps)):
         reset()
@@ -828,6 +834,9 @@ def main():
     ap.add_argument("--eps", type=float, default=1e-12, help="--mode adjoint: CG tolerance")
     ap.add_argument("--ref-cells", type=int, default=32,
                     help="--mode adjoint: side of the FP64 reference-gradient problem")
+    ap.add_argument("--batch-launch", default="auto", choices=["auto", "kernels", "persistent"],
+                    help="--mode batch: the autotuner's launch mode, or three kernels per "
+                         "CG iteration, or one persistent launch per graph replay")
     ap.add_argument("--sequential", type=int, default=32,
                     help="--mode batch: problems also run one by one for comparison")
     args = ap.parse_args()

@@ -845,9 +845,9 @@ __global__ void __launch_bounds__(kBlock) k_finalise(Dev d, Red red) {
 }
 
 // field_summary, field_summary_cl.cl:3-43 (energy argument bound to energy1,
-// ocl_kernels.cpp:466-469); the same arithmetic in both forms.  The three
-// products feed no fused multiply-add, so they run on the integer pipes
-// (tea_emu.cuh, the same bits): the kernel was bound by the FP64 pipe.
+// ocl_kernels.cpp:466-469); the same arithmetic in both forms.  (Its three
+// products on the integer pipes measured slower: 266 -> 457 us at 4096^2,
+// 80 -> 94 registers and three blocks per SM -> two.)
 template <int TH, int F>
 __global__ void __launch_bounds__(kBlock, 1) k_field_summary(Dev d, Red red) {
   tile_driver<TH, 4>(d, red, [&](int x, int y0, bool xin, double* acc) {
@@ -858,11 +858,11 @@ __global__ void __launch_bounds__(kBlock, 1) k_field_summary(Dev d, Red red) {
       if (xin && y < d.y_max) {
         const long long c = cidx(d, x, y);
         const double cell_vol = d.volume[c];
-        const double cell_mass = emu_dmul(cell_vol, d.density[c]);
+        const double cell_mass = cell_vol * d.density[c];
         v0 = cell_vol;
         v1 = cell_mass;
-        v2 = emu_dmul(cell_mass, d.energy1[c]);
-        v3 = emu_dmul(cell_mass, d.u[c]);
+        v2 = cell_mass * d.energy1[c];
+        v3 = cell_mass * d.u[c];
       }
       acc[0] = acc[0] + v0;
       acc[1] = acc[1] + v1;
