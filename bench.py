@@ -503,6 +503,64 @@ def mixed_summary(args):
             "timing": "wall time per timestep, CUDA-synchronised, summed"}
 
 
+def deck_rate(deck, warm_steps, timed_steps, mode):
+    """Runs warm_steps untimed then timed_steps timesteps of a deck on the
+    GPU driver; cell-iterations/s (outer + inner) with CUDA events."""
+    from tealeaf_opencl_gb300 import lib
+    L = lib.load()
+    drv = lib.Driver(deck, mode=mode)
+    for _ in range(warm_steps):
+        drv.step()
+    L.tea_gb300_synchronize()
+    L.tea_gb300_event_record(2)
+    infos = [drv.step() for _ in range(timed_steps)]
+    L.tea_gb300_event_record(3)
+    L.tea_gb300_synchronize()
+    ms = float(L.tea_gb300_event_elapsed_ms(2, 3))
+    x, y = lib.chunk_shape()[:2]
+    drv.close()
+    L.tea_gb300_finalise()
+    its = sum(i.iterations + i.inner_iterations for i in infos)
+    return {"cell_iters_per_s": its * x * y / (ms / 1e3), "ms_per_step": ms / timed_steps,
+            "iterations": [i.iterations for i in infos],
+            "inner_iterations": [i.inner_iterations for i in infos],
+            "warm_steps": warm_steps, "timed_steps": timed_steps}
+
+
+def other_workloads(args):
+    """The benchmark set's other workloads, each measured compactly so that
+    the default line carries them all: 512^2 CG + diagonal Jacobi (10 timed
+    steps after 10, the resident driver), the Chebyshev solve at 4096^2
+    (block Jacobi, 2 timed steps after the one with the eigenvalue
+    estimate), the 512-problem batch (autotuned, 5 steps) and the adjoint at
+    2048^2 (20 steps, checked on 2 finite-difference directions here, 16
+    with --mode adjoint, and on the FP64 reference gradient at 32^2)."""
+    from tealeaf_opencl_gb300 import lib
+    out = {}
+    c1 = deck_rate(deck_for("cg512", 20), 10, 10, lib.DRIVER_RESIDENT)
+    c1["workload"] = "512^2 five-state, CG + jac_diag, tl_eps 1e-15, 10 timed steps after 10"
+    out["cg512"] = c1
+    c2 = deck_rate(deck_for("cheby4096", 3), 1, 2, lib.DRIVER_PER_CALL)
+    c2["workload"] = ("4096^2 five-state, Chebyshev + block Jacobi, 20 CG presteps, "
+                      "tl_eps 1e-15, 2 timed steps after the first")
+    out["cheby4096"] = c2
+    batch = run_batch(argparse.Namespace(problems=512, seed=0, steps=5, reps=1, sequential=0,
+                                         batch_launch="auto"))
+    out["batch512"] = {k: batch[k] for k in ("problems", "cells", "steps", "launch",
+                                            "cell_iters_per_s", "solve_gbs",
+                                            "solve_frac_of_measured_hbm",
+                                            "iterations_per_step")}
+    adj = run_adjoint(argparse.Namespace(cells=2048, steps=20, eps=1e-12, directions=2,
+                                         fd_step=1e-6, seed=0, ref_cells=32))
+    out["adjoint2048"] = {"cells": adj["cells"], "steps": adj["steps"],
+                         "forward_ms": adj["forward_ms"], "backward_ms": adj["backward_ms"],
+                         "backward_over_forward": adj["backward_over_forward"],
+                         "fd_max_rel_err": adj["finite_differences"]["max_rel_err"],
+                         "fd_directions": adj["finite_differences"]["directions"],
+                         "fp64_reference": adj["fp64_reference"]}
+    return out
+
+
 def mixed_compare(cells, steps, lognormal, mixed_solver, inner_steps, presteps):
     from tealeaf_opencl_gb300 import decks, lib
     L = lib.load()
@@ -804,6 +862,9 @@ def main():
     ap.add_argument("--inner-pairs", type=int, default=0, choices=[0, 1],
                     help="PPCG inner steps two at a time in one TMA-fed pass (1) or one "
                          "update_r + calc_sd launch pair per step (0, the faster on GB300)")
+    ap.add_argument("--no-other-workloads", action="store_true",
+                    help="leave out the compact cg512 / cheby4096 / batch / adjoint measurements "
+                         "of the default line")
     ap.add_argument("--no-mixed", action="store_true",
                     help="leave out the mixed-precision comparison of the default line")
     ap.add_argument("--cap", type=int, default=0,
@@ -873,6 +934,8 @@ def main():
     out = run_ours(args, dist)
     if dist.world == 1 and not args.no_mixed:
         out["mixed"] = mixed_summary(args)
+    if dist.world == 1 and not args.no_other_workloads:
+        out["other_workloads"] = other_workloads(args)
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         value, sample, threads = cpu_sample(args.workload, args)
         out["cpu_baseline"] = {"value": value, "unit": "cell-iters/s", "cores": threads,
