@@ -712,37 +712,99 @@ __global__ void __launch_bounds__(kBlock)
 }
 
 // tea_leaf_ppcg_solve_calc_sd for the block-Jacobi preconditioner alone
-// (tea_leaf_ppcg_cl.cl:90-134): k_ppcg_sd's mode-1 block path with no
-// other path compiled in, so it needs fewer registers and more warps fit
-// on an SM to hide the latency of each strip's dependent sweep.  The
-// sweep's multiplies by bfp and the product beta z run on the integer
-// pipes (tea_emu.cuh, bit-identical): 157.6 -> 145.3 us at 4096^2, and
-// 141.6 us with 6 blocks per SM (158.5 with 4).
-constexpr int kSdMinBlocks = 6;
-template <int TH, int F, int MB>
-__global__ void __launch_bounds__(kBlock, MB)
-    k_ppcg_calc_sd_block(Dev d, Red red, double alpha, double beta, const ResState* st) {
+// (tea_leaf_ppcg_cl.cl:90-134, the strip solve of tea_block_jacobi.cl:44-76):
+// z = M^-1 r strip by strip, sd = alpha sd + beta z.  It takes no sum, so
+// its walk over the grid is free: a warp takes 64 columns of one 4-row strip
+// and each lane two adjacent columns, with 16-byte loads (padded column H
+// of every row is 256-byte aligned and the lane's first column is even).
+// Strips cut by the top of the interior, a last odd column and the exact
+// form (whose first-row division needs more registers) take the one-column
+// path.  The product beta z runs on the integer pipes
+// (tea_emu.cuh, bit-identical); the sweep's multiplies by bfp stay on the
+// FP64 pipe, where they sit on the strip's dependent chain.  At 4096^2 on
+// non-zero fields: 149.8 us for one column per lane with both products on
+// the integer pipes, 137.4 with beta z alone there, 131.5 for two columns
+// per lane (165.4 with beta z on the FP64 pipe too).
+constexpr int kSdMinBlocks = 4;
+constexpr int kSdColsPerWarp = 64;
+
+// warp units (64 columns x one strip) of calc_sd, and the blocks they fill
+__host__ __device__ inline long long sd_units(const Dev& d) {
+  return (long long)((d.x_max + kSdColsPerWarp - 1) / kSdColsPerWarp) * ((d.y_max + 3) / 4);
+}
+static int sd_blocks(const Dev& d) {
+  return (int)std::max<long long>(1, (sd_units(d) + kBlock / 32 - 1) / (kBlock / 32));
+}
+
+// the sd update of one cell from the strip's z
+template <int F>
+__device__ __forceinline__ double sd_update(double alpha, double s, double beta, double z) {
+  return F ? __fma_rn(alpha, s, emu_dmul(beta, z)) : alpha * s + emu_dmul(beta, z);
+}
+
+template <int F>
+__global__ void __launch_bounds__(kBlock, kSdMinBlocks)
+    k_ppcg_calc_sd_block(Dev d, double alpha, double beta, const ResState* st) {
   if (st && *(volatile const int*)&st->stop) return;
-  tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
-    if (!xin) return;
-#pragma unroll 1
-    for (int ys = y0; ys < y0 + TH && ys < d.y_max; ys += 4) {
-      double zl[4], rl[4], sv[4];
-      const long long c0 = cidx(d, x, ys);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nux = (d.x_max + kSdColsPerWarp - 1) / kSdColsPerWarp;
+  const long long units = sd_units(d);
+  const long long S = d.S;
+  const double* __restrict__ rp = d.r;
+  double* __restrict__ sp = d.sd;
+  for (long long u = (long long)blockIdx.x * (kBlock / 32) + warp; u < units;
+       u += (long long)gridDim.x * (kBlock / 32)) {
+    const int ty = (int)(u / nux), tx = (int)(u - (long long)ty * nux);
+    const int x = tx * kSdColsPerWarp + 2 * lane, ys = ty * 4;
+    if (x >= d.x_max) continue;
+    const long long c0 = cidx(d, x, ys);
+    const int upper = strip_rows(d, ys);
+    if (F && upper == 4 && ys + 3 < d.y_max && x + 1 < d.x_max) {
+      double ra[4], rb[4], ba[4], bb[4], ka[4], kb[4], ca[4], cb[4], za[4], zb[4];
 #pragma unroll
       for (int i = 0; i < 4; i++) {
-        const bool in = ys + i < d.y_max;
-        rl[i] = in ? d.r[c0 + i * d.S] : 0.0;
-        sv[i] = in ? d.sd[c0 + i * d.S] : 0.0;
+        const double2 rv = *(const double2*)(rp + c0 + i * S);
+        const double2 bv = __ldg((const double2*)(d.bfp + c0 + i * S));
+        const double2 kv =
+            i > 0 ? __ldg((const double2*)(d.Ky + c0 + i * S)) : make_double2(0.0, 0.0);
+        const double2 cv =
+            i < 3 ? __ldg((const double2*)(d.cp + c0 + i * S)) : make_double2(0.0, 0.0);
+        ra[i] = rv.x;
+        rb[i] = rv.y;
+        ba[i] = bv.x;
+        bb[i] = bv.y;
+        ka[i] = kv.x;
+        kb[i] = kv.y;
+        ca[i] = cv.x;
+        cb[i] = cv.y;
       }
-      strip_solve<F, true>(d, c0, strip_rows(d, ys), rl, zl);
+      strip_solve_v<F, false, true>(4, ra, ba, ka, ca, 0.0, za);
+      strip_solve_v<F, false, true>(4, rb, bb, kb, cb, 0.0, zb);
 #pragma unroll
-      for (int i = 0; i < 4; i++)
-        if (ys + i < d.y_max)
-          d.sd[c0 + i * d.S] = F ? __fma_rn(alpha, sv[i], emu_dmul(beta, zl[i]))
-                                 : alpha * sv[i] + emu_dmul(beta, zl[i]);
+      for (int i = 0; i < 4; i++) {
+        const double2 s = *(const double2*)(sp + c0 + i * S);
+        double2 o;
+        o.x = sd_update<F>(alpha, s.x, beta, za[i]);
+        o.y = sd_update<F>(alpha, s.y, beta, zb[i]);
+        *(double2*)(sp + c0 + i * S) = o;
+      }
+    } else {
+      for (int k = 0; k < 2 && x + k < d.x_max; k++) {
+        const long long cc = c0 + k;
+        double zl[4], rl[4], sv[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const bool in = ys + i < d.y_max;
+          rl[i] = in ? rp[cc + i * S] : 0.0;
+          sv[i] = in ? sp[cc + i * S] : 0.0;
+        }
+        strip_solve<F>(d, cc, upper, rl, zl);
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+          if (ys + i < d.y_max) sp[cc + i * S] = sd_update<F>(alpha, sv[i], beta, zl[i]);
+      }
     }
-  });
+  }
 }
 
 // tea_leaf_ppcg_solve_update_r, tea_leaf_ppcg_cl.cl:62-88
@@ -1023,15 +1085,16 @@ void launch_ppcg_calc_sd(Chunk& c, double alpha, double beta) {
   if (c.prec == PREC_JAC_BLOCK) {
     const Dev d4 = dev4(c);
     const char* name = "tea_leaf_ppcg_solve_calc_sd";
+    const int nb = sd_blocks(d4);
     if (c.arith == 2)
-      launch_tile_ns(c, name, d4.ns, k_ppcg_calc_sd_block<4, 2, kSdMinBlocks>, d4, c.red(),
-                     alpha, beta, (const ResState*)nullptr);
+      launch_tile_ns(c, name, nb, k_ppcg_calc_sd_block<2>, d4, alpha, beta,
+                     (const ResState*)nullptr);
     else if (c.arith == 1)
-      launch_tile_ns(c, name, d4.ns, k_ppcg_calc_sd_block<4, 1, kSdMinBlocks>, d4, c.red(),
-                     alpha, beta, (const ResState*)nullptr);
+      launch_tile_ns(c, name, nb, k_ppcg_calc_sd_block<1>, d4, alpha, beta,
+                     (const ResState*)nullptr);
     else
-      launch_tile_ns(c, name, d4.ns, k_ppcg_calc_sd_block<4, 0, kSdMinBlocks>, d4, c.red(),
-                     alpha, beta, (const ResState*)nullptr);
+      launch_tile_ns(c, name, nb, k_ppcg_calc_sd_block<0>, d4, alpha, beta,
+                     (const ResState*)nullptr);
     return;
   }
   TH4_DISPATCH(c, "tea_leaf_ppcg_solve_calc_sd", k_ppcg_sd, dev4(c), c.red(), 1,
@@ -1328,7 +1391,7 @@ static void enqueue_ppcg_iterations_t(Chunk& c, int iters) {
     const int gw = tile_grid(c, k_cg_calc_w<TH, F>);
     const int gu = tile_grid(c, k_ppcg_ur_sd<TH, F>);
     const int gr = tile_grid(c, k_ppcg_update_r<4, F>, d4v[0].ns);
-    const int gs = tile_grid(c, k_ppcg_calc_sd_block<4, F, kSdMinBlocks>, d4v[0].ns);
+    const int gs = tile_grid(c, k_ppcg_calc_sd_block<F>, sd_blocks(d4v[0]));
     const int gz = tile_grid(c, k_ppcg_rz_step<TH, F>);
     const int gp = tile_grid(c, k_cg_calc_p<4, F>, d4v[0].ns);
     int cur = 0;
@@ -1342,8 +1405,8 @@ static void enqueue_ppcg_iterations_t(Chunk& c, int iters) {
       }
       if (k < c.n_ppcg) {
         k_ppcg_update_r<4, F><<<gr, kBlock, 0, c.stream>>>(d4v[cur], red, st);
-        k_ppcg_calc_sd_block<4, F, kSdMinBlocks><<<gs, kBlock, 0, c.stream>>>(
-            d4v[cur], red, c.ppcg_alpha_h[k], c.ppcg_beta_h[k], st);
+        k_ppcg_calc_sd_block<F><<<gs, kBlock, 0, c.stream>>>(
+            d4v[cur], c.ppcg_alpha_h[k], c.ppcg_beta_h[k], st);
       }
       k_ppcg_rz_step<TH, F><<<gz, kBlock, 0, c.stream>>>(dv[cur], red, st);
       k_cg_calc_p<4, F><<<gp, kBlock, 0, c.stream>>>(d4v[cur], red, 0.0, st, c.res_counter);
@@ -1359,7 +1422,7 @@ static void enqueue_ppcg_iterations_t(Chunk& c, int iters) {
   const int gu = tile_grid(c, k_ppcg_ur_sd<TH, F>);
   const int gr = tile_grid(c, k_ppcg_update_r<4, F>, d4.ns);
   const bool blk = c.prec == PREC_JAC_BLOCK;
-  const int gs = blk ? tile_grid(c, k_ppcg_calc_sd_block<4, F, kSdMinBlocks>, d4.ns)
+  const int gs = blk ? tile_grid(c, k_ppcg_calc_sd_block<F>, sd_blocks(d4))
                      : tile_grid(c, k_ppcg_sd<4, F>, d4.ns);
   const int gz = tile_grid(c, k_ppcg_rz_step<TH, F>);
   const int gp = tile_grid(c, k_cg_calc_p<4, F>, d4.ns);
@@ -1369,8 +1432,8 @@ static void enqueue_ppcg_iterations_t(Chunk& c, int iters) {
     for (int k = 0; k < c.n_ppcg; k++) {
       k_ppcg_update_r<4, F><<<gr, kBlock, 0, c.stream>>>(d4, red, st);
       if (blk)
-        k_ppcg_calc_sd_block<4, F, kSdMinBlocks><<<gs, kBlock, 0, c.stream>>>(
-            d4, red, c.ppcg_alpha_h[k], c.ppcg_beta_h[k], st);
+        k_ppcg_calc_sd_block<F><<<gs, kBlock, 0, c.stream>>>(
+            d4, c.ppcg_alpha_h[k], c.ppcg_beta_h[k], st);
       else
         k_ppcg_sd<4, F><<<gs, kBlock, 0, c.stream>>>(d4, red, 1, div_const(1.0), c.ppcg_alpha_h[k],
                                                      c.ppcg_beta_h[k], st);

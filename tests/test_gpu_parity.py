@@ -45,6 +45,9 @@ CASES = [
     # defined (p.w = 0); the set-up, norms and summaries are still compared
     (1, 1, 1, "cg", "jac_diag", {"cg_iters": 0}),
     (3, 5, 2, "ppcg", "jac_block", {}),
+    # odd width (a last single column in calc_sd's two-column walk) and, with
+    # halo 1, a top strip of 3 interior rows that BLOCK_TOP counts as 4
+    (97, 67, 1, "ppcg", "jac_block", {}),
     (33, 17, 1, "cg", "jac_block", {"reflective": True}),
     (33, 18, 2, "chebyshev", "jac_block", {"reflective": True}),
     (40, 23, 1, "jacobi", "none", {"reflective": True, "coef": 2}),
