@@ -530,9 +530,9 @@ def deck_rate(deck, warm_steps, timed_steps, mode):
 def other_workloads(args):
     """The benchmark set's other workloads, each measured compactly so that
     the default line carries them all: 512^2 CG + diagonal Jacobi (10 timed
-    steps after 10, the resident driver), the Chebyshev solve at 4096^2
-    (block Jacobi, 2 timed steps after the one with the eigenvalue
-    estimate), the 512-problem batch (autotuned, 5 steps) and the adjoint at
+    steps after 10), the Chebyshev solve at 4096^2 (block Jacobi, 2 timed
+    steps after the one with the eigenvalue estimate), both through the
+    resident driver, the 512-problem batch (autotuned, 5 steps) and the adjoint at
     2048^2 (20 steps, checked on 2 finite-difference directions here, 16
     with --mode adjoint, and on the FP64 reference gradient at 32^2)."""
     from tealeaf_opencl_gb300 import lib
@@ -540,7 +540,7 @@ def other_workloads(args):
     c1 = deck_rate(deck_for("cg512", 20), 10, 10, lib.DRIVER_RESIDENT)
     c1["workload"] = "512^2 five-state, CG + jac_diag, tl_eps 1e-15, 10 timed steps after 10"
     out["cg512"] = c1
-    c2 = deck_rate(deck_for("cheby4096", 3), 1, 2, lib.DRIVER_PER_CALL)
+    c2 = deck_rate(deck_for("cheby4096", 3), 1, 2, lib.DRIVER_RESIDENT)
     c2["workload"] = ("4096^2 five-state, Chebyshev + block Jacobi, 20 CG presteps, "
                       "tl_eps 1e-15, 2 timed steps after the first")
     out["cheby4096"] = c2
