@@ -158,6 +158,12 @@ class Dist:
             self.pg.destroy_process_group()
 
 
+def whole_job_rate(dist, cell_iters, seconds):
+    """Cell-iterations per second of the whole job: every rank's count
+    summed, over the slowest rank's time (replicas run the same work)."""
+    return dist.sum(cell_iters) / dist.max(seconds)
+
+
 # ---------------------------------------------------------------------------
 # clocks sampled during the timed region
 # ---------------------------------------------------------------------------
@@ -278,8 +284,7 @@ def run_ours(args, dist):
     outer = sum(i.iterations for i in infos)
     inner = sum(i.inner_iterations for i in infos)
     ms_max = dist.max(ms)
-    total_all = dist.sum(outer + inner)
-    value = total_all * ncell / (ms_max / 1e3)
+    value = whole_job_rate(dist, (outer + inner) * ncell, ms / 1e3)
 
     # ---- e2e: per-call C ABI, host buffers, copies inside the timed region ----
     drv = lib.Driver(deck, mode=lib.DRIVER_PER_CALL, max_iters_cap=args.cap)
@@ -317,7 +322,7 @@ def run_ours(args, dist):
     drv.close()
     for b in bufs:
         L.tea_gb300_host_free(b)
-    e2e_value = dist.sum(e2e_outer) * ncell / dist.max(e2e_s)
+    e2e_value = whole_job_rate(dist, e2e_outer * ncell, e2e_s)
 
     peak, peak_kind = measured_peak_hbm()
     avg_launch_ms = kms.value / kn.value if kn.value else None
