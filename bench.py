@@ -83,14 +83,19 @@ FP64_PER_CELL = {
     ("tea_leaf_cg_solve_calc_ur", "jac_diag", "exact"): 7,
     ("tea_leaf_cg_solve_calc_ur", "jac_block", "chain"): 5.5,
     ("tea_leaf_cg_solve_calc_ur", "jac_block", "fused"): 5.5,
+    # the Chebyshev step: operator 5 (chain) or 6 (fused), r = u0 - w 1,
+    # strip sweep 2.5, alpha p + beta z 1 (beta z on the integer pipes)
+    ("tea_leaf_cheby_solve_calc_p", "jac_block", "chain"): 9.5,
+    ("tea_leaf_cheby_solve_calc_p", "jac_block", "fused"): 10.5,
 }
 
 
 def deck_for(name, steps):
     from tealeaf_opencl_gb300 import decks
     cells, solver, prec, halo, inner, presteps, eps = WORKLOADS[name][:7]
-    # C1 names tl_max_iters 5000; the 4096^2 configuration names none, so
-    # the reference's default of 1000 (read_input.f90:59) applies
+    # the 512^2 CG configuration names tl_max_iters 5000; the 4096^2 one
+    # names none, so the reference's default of 1000 (read_input.f90:59)
+    # applies
     max_iters = 5000 if cells <= 512 else 1000
     return decks.five_state_deck(cells, solver=solver, prec=prec, steps=steps,
                                  eps=eps, max_iters=max_iters, halo=halo,

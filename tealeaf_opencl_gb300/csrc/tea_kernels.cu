@@ -505,8 +505,10 @@ __device__ __forceinline__ double cheby_update(double a, double p, double bl,
 // tea_leaf_cheby_solve_calc_p with the block-Jacobi preconditioner alone
 // (tea_leaf_cheby_cl.cl:78-145): k_cheby_p's mode-1 block path with no
 // other path compiled in: 72 registers against 80, 340 -> 326 us at 4096^2.
-// (The integer-pipe products, in the operator or the sweep, made it slower
-// here: 352 and 388 us.)
+// The product beta z runs on the integer pipes (tea_emu.cuh, bit-identical):
+// on non-zero fields 340.2 -> 315.6 us.  The operator's first product there
+// as well was slower (367.0 us), and so were the sweep's multiplies by bfp
+// (388 us), which sit on each strip's dependent chain.
 template <int TH, int F>
 __global__ void __launch_bounds__(kBlock, 3)
     k_cheby_calc_p_block(Dev d, Red red, double alpha, double beta) {
@@ -535,7 +537,9 @@ __global__ void __launch_bounds__(kBlock, 3)
       strip_solve<F>(d, c0, strip_rows(d, ys), rl, zl);
 #pragma unroll
       for (int i = 0; i < 4; i++)
-        if (ys + i < d.y_max) d.p[c0 + i * d.S] = cheby_update<F>(alpha, pl[i], beta, zl[i]);
+        if (ys + i < d.y_max)
+          d.p[c0 + i * d.S] = F ? __fma_rn(alpha, pl[i], emu_dmul(beta, zl[i]))
+                                : alpha * pl[i] + emu_dmul(beta, zl[i]);
     }
   });
 }
