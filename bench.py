@@ -53,7 +53,7 @@ WORKLOADS = {
     "ppcg4096": (4096, "ppcg", "jac_block", 2, 10, 20, 1e-15,
                  "tea_leaf_ppcg_solve_update_r", 56),
     "cheby4096": (4096, "chebyshev", "jac_block", 2, 10, 20, 1e-15,
-                  "tea_leaf_cheby_solve_calc_p", 72),
+                  "tea_leaf_cheby_solve_calc_p_u", 104),
     "cg4096": (4096, "cg", "jac_block", 2, 10, 20, 1e-15,
                "tea_leaf_cg_solve_calc_ur", 64),
     "cg512": (512, "cg", "jac_diag", 1, 10, 25, 1e-15,
@@ -87,6 +87,9 @@ FP64_PER_CELL = {
     # strip sweep 2.5, alpha p + beta z 1 (beta z on the integer pipes)
     ("tea_leaf_cheby_solve_calc_p", "jac_block", "chain"): 9.5,
     ("tea_leaf_cheby_solve_calc_p", "jac_block", "fused"): 10.5,
+    # the same with calc_u's u + p folded in
+    ("tea_leaf_cheby_solve_calc_p_u", "jac_block", "chain"): 10.5,
+    ("tea_leaf_cheby_solve_calc_p_u", "jac_block", "fused"): 11.5,
 }
 
 
@@ -391,6 +394,8 @@ KERNEL_BYTES = {
     "tea_leaf_ppcg_solve_calc_sd": {"jac_diag": 32, "jac_block": 56, "none": 24},
     "tea_leaf_cheby_solve_calc_p": {"jac_diag": 80, "jac_block": 96, "none": 72},
     "tea_leaf_cheby_solve_calc_u": 24,
+    # calc_p and calc_u in one pass (block Jacobi): calc_p's fields and u written
+    "tea_leaf_cheby_solve_calc_p_u": {"jac_diag": 88, "jac_block": 104, "none": 80},
     "tea_leaf_calc_residual": 48,         # u0 u Kx Ky (diag), r
     "tea_leaf_cg_solve_init_p": {"jac_diag": 32, "jac_block": 56, "none": 24},
     "tea_leaf_ppcg_solve_init_sd": {"jac_diag": 24, "jac_block": 48, "none": 16},

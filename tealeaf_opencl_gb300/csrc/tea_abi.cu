@@ -231,7 +231,8 @@ static void free_chunk(Chunk& c) {
   c.cheby_alpha_h = c.cheby_beta_h = c.ppcg_alpha_h = c.ppcg_beta_h = nullptr;
   cudaFree(c.r2.base);
   cudaFree(c.sd2.base);
-  c.r2 = c.sd2 = Field();
+  cudaFree(c.u2.base);
+  c.r2 = c.sd2 = c.u2 = Field();
   c.pending_inner = -1;
   tb_release();
   if (c.stream) cudaStreamDestroy(c.stream);
@@ -406,6 +407,8 @@ bool ensure_alt_fields(Chunk& c) {
          check_cuda(cudaMemcpyAsync(c.sd2.base, c.sd.base, n, cudaMemcpyDeviceToDevice, c.stream),
                     "alt sd copy");
 }
+
+bool ensure_u_alt(Chunk& c) { return c.u2.base || alloc_field(c, c.u2); }
 
 void swap_alt_fields(Chunk& c) {
   std::swap(c.r, c.r2);
@@ -730,6 +733,15 @@ extern "C" void tea_leaf_cheby_iterate_kernel_ocl_(const int* cheby_calc_step) {
   if (s < 0 || s >= c.n_cheby) {
     fail(11, "Chebyshev step %d outside the %d stored coefficients",
          *cheby_calc_step, c.n_cheby);
+    return;
+  }
+  if (c.prec == PREC_JAC_BLOCK) {
+    // calc_u folded into calc_p: the new u goes to the second buffer,
+    // which then becomes u
+    if (!ensure_u_alt(c)) return;
+    launch_cheby_calc_pu(c, c.cheby_alpha_h[s], c.cheby_beta_h[s], c.u2.f);
+    std::swap(c.u, c.u2);
+    c.field_epoch++;
     return;
   }
   launch_cheby_calc_p(c, c.cheby_alpha_h[s], c.cheby_beta_h[s]);

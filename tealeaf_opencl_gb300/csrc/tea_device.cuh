@@ -550,6 +550,30 @@ __device__ __forceinline__ bool tile_driver_p1(const Dev& d, const Red& red,
   return tile_driver<TH, NV, Body, 1>(d, red, body);
 }
 
+// Copies the halo ring of a field (every padded cell outside the interior,
+// depth H) from src to dst; grid-stride over all threads of the launch.
+__device__ __forceinline__ void copy_halo_ring(const Dev& d, const double* src, double* dst) {
+  const int H = d.H, xs = d.x_max + 2 * H;
+  const long long band = (long long)H * xs;  // the rows above or below
+  const long long n = 2 * band + 2LL * H * d.y_max;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    int row, col;
+    if (i < 2 * band) {
+      const long long j = i < band ? i : i - band;
+      row = (int)(j / xs) + (i < band ? 0 : H + d.y_max);
+      col = (int)(j % xs);
+    } else {
+      const long long j = i - 2 * band;
+      const int k = (int)(j % (2 * H));
+      row = H + (int)(j / (2 * H));
+      col = k < H ? k : d.x_max + k;
+    }
+    const long long o = (long long)row * d.S + col;
+    dst[o] = src[o];
+  }
+}
+
 // True in the last block of the grid to get here (counter reset after).
 __device__ __forceinline__ bool last_block(unsigned int* counter) {
   __shared__ unsigned int is_last;

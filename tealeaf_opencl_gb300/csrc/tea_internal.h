@@ -130,6 +130,10 @@ struct Chunk {
   // (tea_ppcg_tb.cu), which writes r and sd to the pair it does not read;
   // allocated on first use, with the halos of the live pair
   Field r2, sd2;
+  // second u buffer of the Chebyshev iteration with calc_u folded into
+  // calc_p (block Jacobi), which writes the new u, halo included, to the
+  // buffer it does not read; the two then trade places
+  Field u2;
   int inner_pairs = 0;      // run PPCG inner steps in fused pairs where they apply
   int field_epoch = 0;      // bumped whenever r/sd and r2/sd2 trade places
   int pending_inner = -1;   // a per-call inner step (0-based) not launched yet
@@ -197,6 +201,9 @@ void launch_cg_calc_p(Chunk& c, double beta);
 void launch_cheby_init_p(Chunk& c, double theta);
 void launch_cheby_calc_p(Chunk& c, double alpha, double beta);
 void launch_cheby_calc_u(Chunk& c);
+// calc_p and calc_u of one Chebyshev iteration in one pass (block Jacobi),
+// the new u into un
+void launch_cheby_calc_pu(Chunk& c, double alpha, double beta, double* un);
 void launch_ppcg_init_sd(Chunk& c, double theta);
 void launch_ppcg_update_r(Chunk& c);
 void launch_ppcg_calc_sd(Chunk& c, double alpha, double beta);
@@ -257,6 +264,8 @@ void tb_release();
 // the second r/sd buffers (tea_abi.cu): allocated and given the live
 // buffers' contents once; false on failure
 bool ensure_alt_fields(Chunk& c);
+// allocates u2 on first use
+bool ensure_u_alt(Chunk& c);
 // r/sd and r2/sd2 trade places (the fused pair has just written r2/sd2)
 void swap_alt_fields(Chunk& c);
 // launches a per-call PPCG inner step held back for pairing (tea_abi.cu)

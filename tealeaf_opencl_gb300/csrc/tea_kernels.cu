@@ -509,20 +509,28 @@ __device__ __forceinline__ double cheby_update(double a, double p, double bl,
 // on non-zero fields 340.2 -> 315.6 us.  The operator's first product there
 // as well was slower (367.0 us), and so were the sweep's multiplies by bfp
 // (388 us), which sit on each strip's dependent chain.
-template <int TH, int F>
-__global__ void __launch_bounds__(kBlock, 3)
-    k_cheby_calc_p_block(Dev d, Red red, double alpha, double beta) {
+// With U it also carries out tea_leaf_cheby_solve_calc_u (u = u + p,
+// tea_leaf_cheby_cl.cl:66-76) on the p it has just formed, writing the new
+// u to un: other blocks still read this block's u for their operator, so u
+// cannot be updated in place.  un then becomes u; the kernel also copies
+// u's halo ring to un, so un is exactly the in-place result.  One FP64 add
+// per cell more in this FP64-bound kernel against a separate pass over u
+// and p: 373.6 -> 350.6 us per iteration at 4096^2 (non-zero fields).
+template <int TH, int F, bool U>
+__device__ __forceinline__ void cheby_block_body(const Dev& d, const Red& red, double alpha,
+                                                 double beta, double* un) {
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
     if (!xin) return;
 #pragma unroll 1
     for (int ys = y0; ys < y0 + TH && ys < d.y_max; ys += 4) {
-      double zl[4], rl[4] = {0.0, 0.0, 0.0, 0.0}, wl[4], pl[4];
+      double zl[4], rl[4] = {0.0, 0.0, 0.0, 0.0}, wl[4], pl[4], ul[4];
       const long long c0 = cidx(d, x, ys);
 #pragma unroll
       for (int i = 0; i < 4; i++) {
         if (ys + i < d.y_max) {
           const long long c = c0 + i * d.S;
           wl[i] = smvp<F, false, false>(d, d.u, c);
+          if (U) ul[i] = d.u[c];
           rl[i] = d.u0[c] - wl[i];
           pl[i] = d.p[c];
         }
@@ -537,11 +545,27 @@ __global__ void __launch_bounds__(kBlock, 3)
       strip_solve<F>(d, c0, strip_rows(d, ys), rl, zl);
 #pragma unroll
       for (int i = 0; i < 4; i++)
-        if (ys + i < d.y_max)
-          d.p[c0 + i * d.S] = F ? __fma_rn(alpha, pl[i], emu_dmul(beta, zl[i]))
-                                : alpha * pl[i] + emu_dmul(beta, zl[i]);
+        if (ys + i < d.y_max) {
+          const double pn = F ? __fma_rn(alpha, pl[i], emu_dmul(beta, zl[i]))
+                              : alpha * pl[i] + emu_dmul(beta, zl[i]);
+          d.p[c0 + i * d.S] = pn;
+          if (U) un[c0 + i * d.S] = ul[i] + pn;
+        }
     }
   });
+}
+
+template <int TH, int F>
+__global__ void __launch_bounds__(kBlock, 3)
+    k_cheby_calc_p_block(Dev d, Red red, double alpha, double beta) {
+  cheby_block_body<TH, F, false>(d, red, alpha, beta, nullptr);
+}
+
+template <int TH, int F>
+__global__ void __launch_bounds__(kBlock, 3)
+    k_cheby_calc_pu_block(Dev d, Red red, double alpha, double beta, double* un) {
+  cheby_block_body<TH, F, true>(d, red, alpha, beta, un);
+  copy_halo_ring(d, d.u, un);
 }
 
 // The Chebyshev residual step shared by tea_leaf_cheby_solve_init_p and
@@ -1069,6 +1093,11 @@ void launch_cheby_calc_p(Chunk& c, double alpha, double beta) {
   }
   TH_DISPATCH(c, "tea_leaf_cheby_solve_calc_p", k_cheby_p, c.dev(), c.red(), 1,
               div_const(1.0), alpha, beta);
+}
+
+void launch_cheby_calc_pu(Chunk& c, double alpha, double beta, double* un) {
+  TH_DISPATCH(c, "tea_leaf_cheby_solve_calc_p_u", k_cheby_calc_pu_block, c.dev(), c.red(),
+              alpha, beta, un);
 }
 
 void launch_cheby_calc_u(Chunk& c) {

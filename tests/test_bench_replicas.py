@@ -39,7 +39,7 @@ def _rank(rank, world, port, out):
 
 def test_two_gloo_ranks_aggregate_the_whole_job():
     world, port = 2, _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_rank, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)

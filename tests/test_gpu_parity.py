@@ -48,6 +48,10 @@ CASES = [
     # odd width (a last single column in calc_sd's two-column walk) and, with
     # halo 1, a top strip of 3 interior rows that BLOCK_TOP counts as 4
     (97, 67, 1, "ppcg", "jac_block", {}),
+    # Chebyshev with block Jacobi writes u to a second buffer, halo ring
+    # included; halo depth 3 and a width and height that are not multiples
+    # of the tiles
+    (45, 37, 3, "chebyshev", "jac_block", {}),
     (33, 17, 1, "cg", "jac_block", {"reflective": True}),
     (33, 18, 2, "chebyshev", "jac_block", {"reflective": True}),
     (40, 23, 1, "jacobi", "none", {"reflective": True, "coef": 2}),
