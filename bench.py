@@ -55,7 +55,7 @@ WORKLOADS = {
     "cheby4096": (4096, "chebyshev", "jac_block", 2, 10, 20, 1e-15,
                   "tea_leaf_cheby_solve_calc_p_u", 104),
     "cg4096": (4096, "cg", "jac_block", 2, 10, 20, 1e-15,
-               "tea_leaf_cg_solve_calc_ur", 64),
+               "tea_leaf_cg_solve_calc_ur", 88),
     "cg512": (512, "cg", "jac_diag", 1, 10, 25, 1e-15,
               "tea_leaf_cg_solve_calc_ur", 64),
 }

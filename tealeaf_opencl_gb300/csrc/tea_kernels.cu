@@ -327,7 +327,10 @@ __global__ void k_update_halo(Dev d, int mask, int depth) {
 // us), cheby calc_u (62.4 -> 59.5), field_summary (277 -> 267),
 // calc_residual (155 -> 153) and cg calc_p (63.3 -> 62.0); slower for
 // calc_ur (240 -> 289), cg init_p (139 -> 196), init_sd, calc_w (186 ->
-// 308) and the Chebyshev step, which keep the plain bound.
+// 308) and the Chebyshev step, which keep the plain bound.  calc_w, with
+// its fields through restrict-qualified pointers (cg_w_tile_r), names 4
+// blocks per SM instead: 64 registers with a 16-byte spill, 192.2 -> 174.4
+// us on non-zero fields (92 registers and 3 blocks per SM without it).
 // ---------------------------------------------------------------------------
 
 // tea_leaf_calc_residual, tea_leaf_common_cl.cl:17-36
@@ -431,11 +434,11 @@ __global__ void __launch_bounds__(kBlock) k_cg_init_p(Dev d, Red red) {
 // (device-resident loop) it does nothing once the loop has stopped and
 // leaves pw in st.
 template <int TH, int F>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 4)
     k_cg_calc_w(Dev d, Red red, ResState* st) {
   if (st && *(volatile int*)&st->stop) return;
   const bool last = tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
-    cg_w_tile<TH, F>(d, x, y0, xin, acc);
+    cg_w_tile_r<TH, F>(d, x, y0, xin, acc);
   });
   if (st && last && threadIdx.x == 0) st->pw = red.result[0];
 }
