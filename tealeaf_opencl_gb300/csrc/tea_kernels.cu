@@ -330,7 +330,9 @@ __global__ void k_update_halo(Dev d, int mask, int depth) {
 // 308) and the Chebyshev step, which keep the plain bound.  calc_w, with
 // its fields through restrict-qualified pointers (cg_w_tile_r), names 4
 // blocks per SM instead: 64 registers with a 16-byte spill, 192.2 -> 174.4
-// us on non-zero fields (92 registers and 3 blocks per SM without it).
+// us on non-zero fields (92 registers and 3 blocks per SM without it).  So
+// do calc_ur and PPCG's calc_ur + init_sd (cg_ur_tile_r): 246.4 -> 210.9
+// and 223.7 -> 215.0 us.
 // ---------------------------------------------------------------------------
 
 // tea_leaf_calc_residual, tea_leaf_common_cl.cl:17-36
@@ -449,14 +451,14 @@ __global__ void __launch_bounds__(kBlock, 4)
 // (cg_scalar_step).  With NV = 2 it also sums r.r, for the resident loop's
 // optional exit test on the unpreconditioned residual.
 template <int TH, int F, int NV = 1>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 4)
     k_cg_calc_ur(Dev d, Red red, double alpha, ResState* st) {
   if (st) {
     if (*(volatile int*)&st->stop) return;
     alpha = st->rro / st->pw;
   }
   const bool last = tile_driver<TH, NV>(d, red, [&](int x, int y0, bool xin, double* acc) {
-    cg_ur_tile<TH, F, NV>(d, x, y0, xin, acc, alpha);
+    cg_ur_tile_r<TH, F, NV>(d, x, y0, xin, acc, alpha);
   });
   if (st && last && threadIdx.x == 0) {
     cg_scalar_step<NV>(st, alpha, red.result);
@@ -468,10 +470,10 @@ __global__ void __launch_bounds__(kBlock)
 // (tea_leaf_ppcg_cl.cl:4-60) from the z it forms, into d.sd (the spare
 // buffer, so the current sd stays as it is until init_sd is called).
 template <int TH, int F>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 4)
     k_cg_calc_ur_sd(Dev d, Red red, double alpha, DivConst theta) {
   tile_driver<TH, 1>(d, red, [&](int x, int y0, bool xin, double* acc) {
-    cg_ur_tile<TH, F, 1, false, true>(d, x, y0, xin, acc, alpha, theta);
+    cg_ur_tile_r<TH, F, 1, true>(d, x, y0, xin, acc, alpha, theta);
   });
 }
 
@@ -1373,12 +1375,12 @@ static bool launch_cg_persistent(Chunk& c) {
 // state, fused with tea_leaf_ppcg_init_sd: PPCG discards this r.z, so no
 // sum is taken, and sd = M^-1 r / theta comes from the z formed here.
 template <int TH, int F>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 4)
     k_ppcg_ur_sd(Dev d, Red red, ResState* st, DivConst theta) {
   if (*(volatile int*)&st->stop) return;
   const double alpha = st->rro / st->pw;
   tile_driver<TH, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
-    cg_ur_tile<TH, F, 0, false, true>(d, x, y0, xin, acc, alpha, theta);
+    cg_ur_tile_r<TH, F, 0, true>(d, x, y0, xin, acc, alpha, theta);
   });
   if (blockIdx.x == 0 && threadIdx.x == 0) st->alpha = alpha;
 }
