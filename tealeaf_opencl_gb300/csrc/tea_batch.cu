@@ -167,10 +167,19 @@ __device__ __forceinline__ void phase_w(const Dev* __restrict__ devs,
     const Red red = reds[i];
     const int s0 = (u - wl.ustart[j]) * wl.G, s1 = min(s0 + wl.G, d.ns);
     unit_partials(d, red, s0, s1, sh, [&](int x, int y0, bool xin, double* a) {
-      if (d.th == 16)
-        cg_w_tile<16, F, CG>(d, x, y0, xin, a);
-      else
-        cg_w_tile<4, F, CG>(d, x, y0, xin, a);
+      // the three-kernel mode takes the restrict-qualified bodies; the
+      // persistent mode reads other blocks' writes through L2 (CG)
+      if constexpr (CG) {
+        if (d.th == 16)
+          cg_w_tile<16, F, CG>(d, x, y0, xin, a);
+        else
+          cg_w_tile<4, F, CG>(d, x, y0, xin, a);
+      } else {
+        if (d.th == 16)
+          cg_w_tile_r<16, F>(d, x, y0, xin, a);
+        else
+          cg_w_tile_r<4, F>(d, x, y0, xin, a);
+      }
     });
     if (unit_done(red.counter, units_of(d.ns, wl.G), is_last)) {
       block_final_sum<1>(red.partials, red.stride, d.ns, red.result, sh);
@@ -199,10 +208,17 @@ __device__ __forceinline__ void phase_ur(const Dev* __restrict__ devs,
     const double alpha = st_load<CG>(&st[i].rro) / st_load<CG>(&st[i].pw);
     const int s0 = (u - wl.ustart[j]) * wl.G, s1 = min(s0 + wl.G, d.ns);
     unit_partials(d, red, s0, s1, sh, [&](int x, int y0, bool xin, double* a) {
-      if (d.th == 16)
-        cg_ur_tile<16, F, 1, CG>(d, x, y0, xin, a, alpha);
-      else
-        cg_ur_tile<4, F, 1, CG>(d, x, y0, xin, a, alpha);
+      if constexpr (CG) {
+        if (d.th == 16)
+          cg_ur_tile<16, F, 1, CG>(d, x, y0, xin, a, alpha);
+        else
+          cg_ur_tile<4, F, 1, CG>(d, x, y0, xin, a, alpha);
+      } else {
+        if (d.th == 16)
+          cg_ur_tile_r<16, F, 1>(d, x, y0, xin, a, alpha);
+        else
+          cg_ur_tile_r<4, F, 1>(d, x, y0, xin, a, alpha);
+      }
     });
     if (unit_done(red.counter, units_of(d.ns, wl.G), is_last)) {
       block_final_sum<1>(red.partials, red.stride, d.ns, red.result, sh);
