@@ -40,6 +40,7 @@ struct MixDev {
   long long S;  // row stride in floats
   float *Kx, *Ky, *D, *Mi, *d, *r, *p, *w;
   float *z, *sd;  // PPCG: the kept M^-1 r and the inner direction
+  float* p2;      // CG with calc_p folded into calc_w: the other p buffer
 };
 
 struct MixState {
@@ -55,12 +56,13 @@ struct MixChunk {
   bool ready = false;
   int x_max = 0, y_max = 0, H = 0;
   long long S = 0;
-  float* base[10] = {nullptr};
+  float* base[11] = {nullptr};
   MixDev dev{};
   MixState* st = nullptr;    // device
   MixState* st_h = nullptr;  // pinned
   unsigned int* counter = nullptr;
   cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph_fused = nullptr;  // CG with calc_p folded into calc_w
   int graph_batch = 0;
   int graph_epoch = 0;  // the chunk's field_epoch at capture
 };
@@ -303,6 +305,112 @@ __global__ void __launch_bounds__(kBlock, 4)
     for (int k = 0; k < 4; k++) v[k] = pair_value(hi[k], lo[k]);
   });
   if (last && threadIdx.x == 0) st->pw = red.result[0];
+}
+
+// calc_p folded into calc_w (CG inner loop of the mixed solve): with the
+// previous iteration's beta, p' = Mi r + beta p (k_mix_calc_p_v4's fused
+// multiply-add per cell) is formed where w = A p' needs it, from the old p,
+// Mi and r: each lane walks its 4 columns down the tile keeping p' of the
+// rows above, at and below, and forms the columns either side itself.
+// Halo cells keep the old p, as calc_p leaves them.  p' is written to pout
+// (other blocks still read the old p for their operator), w and p'.w as
+// k_mix_calc_w4.  On the first iteration of an inner solve (no calc_p
+// pending) p' is p.  In FP32 the extra multiply-adds are cheap; the pass
+// over p, Mi and r that calc_p made disappears with its launch.
+template <int TH>
+__global__ void __launch_bounds__(kBlock, 4)
+    k_mix_calc_pw4(Dev d, MixDev m, float* pout, Red red, MixState* st) {
+  if (*(volatile int*)&st->stop) return;
+  const bool pend = *(volatile int*)&st->p_pending != 0;
+  const float bf = (float)st->beta;
+  const bool last = quad_driver<TH>(d, red, [&](int x, int y0, double* v) {
+    const long long S = m.S;
+    const float* __restrict__ pin = m.p;
+    const float* __restrict__ mi = m.Mi;
+    const float* __restrict__ rr = m.r;
+    float* __restrict__ w = m.w;
+    float* __restrict__ po = pout;
+    // p' of one interior cell, or the old p elsewhere
+    auto pn1 = [&](long long c, int xx, int y) -> float {
+      const float pv = pin[c];
+      if (!pend || xx < 0 || xx >= d.x_max || y < 0 || y >= d.y_max) return pv;
+      return __fmaf_rn(bf, pv, mi[c] * rr[c]);
+    };
+    float hi[4] = {0.0f, 0.0f, 0.0f, 0.0f}, lo[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (x + 4 <= d.x_max) {
+      // p' of the 4 columns at row y (a halo row keeps the old p)
+      auto pn4 = [&](long long c, int y) -> float4 {
+        const float4 pv = ld4(pin + c);
+        if (!pend || y < 0 || y >= d.y_max) return pv;
+        const float4 m4 = ld4(mi + c), r4 = ld4(rr + c);
+        return make_float4(__fmaf_rn(bf, pv.x, m4.x * r4.x), __fmaf_rn(bf, pv.y, m4.y * r4.y),
+                           __fmaf_rn(bf, pv.z, m4.z * r4.z), __fmaf_rn(bf, pv.w, m4.w * r4.w));
+      };
+      const long long cb = cidx32(d, m, x, y0);
+      float4 ps = pn4(cb - S, y0 - 1), pc = pn4(cb, y0);
+#pragma unroll 1
+      for (int j = 0; j < TH; j++) {
+        const int y = y0 + j;
+        float pv[4] = {0.0f, 0.0f, 0.0f, 0.0f}, wv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (y < d.y_max) {
+          const long long c = cb + j * S;
+          const float4 pnr = pn4(c + S, y + 1);
+          const float4 kx = ld4(m.Kx + c), kyc = ld4(m.Ky + c), kyn = ld4(m.Ky + c + S);
+          const float4 D = ld4(m.D + c);
+          const float pwst = pn1(c - 1, x - 1, y), peas = pn1(c + 4, x + 4, y);
+          const float kx4 = m.Kx[c + 4];
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            const float xw = k == 0 ? pwst : f4(pc, k - 1);
+            const float xe = k == 3 ? peas : f4(pc, k + 1);
+            const float ke = k == 3 ? kx4 : f4(kx, k + 1);
+            const float t1 = __fmaf_rn(f4(kyc, k), f4(ps, k), f4(kyn, k) * f4(pnr, k));
+            const float t2 = __fmaf_rn(f4(kx, k), xw, ke * xe);
+            wv[k] = __fmaf_rn(f4(D, k), f4(pc, k), -t1) - t2;
+            pv[k] = f4(pc, k);
+          }
+          *reinterpret_cast<float4*>(w + c) = make_float4(wv[0], wv[1], wv[2], wv[3]);
+          *reinterpret_cast<float4*>(po + c) = pc;
+          ps = pc;
+          pc = pnr;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) acc_pair(hi[k], lo[k], pv[k], wv[k]);
+      }
+    } else {
+#pragma unroll 1
+      for (int j = 0; j < TH; j++) {
+        const int y = y0 + j;
+        float pv[4] = {0.0f, 0.0f, 0.0f, 0.0f}, wv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (y < d.y_max) {
+          const long long c = cidx32(d, m, x, y);
+#pragma unroll
+          for (int k = 0; k < 4; k++)
+            if (x + k < d.x_max) {
+              const long long ck = c + k;
+              const float pc = pn1(ck, x + k, y);
+              const float t1 = __fmaf_rn(__ldg(m.Ky + ck), pn1(ck - S, x + k, y - 1),
+                                         __ldg(m.Ky + ck + S) * pn1(ck + S, x + k, y + 1));
+              const float t2 = __fmaf_rn(__ldg(m.Kx + ck), pn1(ck - 1, x + k - 1, y),
+                                         __ldg(m.Kx + ck + 1) * pn1(ck + 1, x + k + 1, y));
+              wv[k] = __fmaf_rn(__ldg(m.D + ck), pc, -t1) - t2;
+              pv[k] = pc;
+              w[ck] = wv[k];
+              po[ck] = pc;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) acc_pair(hi[k], lo[k], pv[k], wv[k]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) v[k] = pair_value(hi[k], lo[k]);
+  });
+  if (last && threadIdx.x == 0) {
+    st->pw = red.result[0];
+    st->p_pending = 0;
+    __threadfence();
+  }
 }
 
 // d += alpha p; r -= alpha w; z = Mi r; r.z and the inner loop's scalar
@@ -600,9 +708,29 @@ static void enqueue_inner(Chunk& c, int iters) {
   }
 }
 
+// The CG inner loop with calc_p folded into calc_w: iteration i reads p
+// from one buffer and writes p' to the other, so an even count ends where
+// it began.
+template <int TH>
+static void enqueue_inner_fused(Chunk& c, int iters) {
+  const Dev d = c.dev();
+  const Red red = c.red();
+  MixDev m[2] = {g_mix.dev, g_mix.dev};
+  m[1].p = g_mix.dev.p2;
+  const int nblk4 = (d.ns + 3) / 4;
+  const int gw = mix_grid(c, k_mix_calc_pw4<TH>, nblk4);
+  const int gu = mix_grid(c, k_mix_calc_ur4<TH>, nblk4);
+  for (int i = 0; i < iters; i++) {
+    const int a = i & 1, b = a ^ 1;
+    k_mix_calc_pw4<TH><<<gw, kBlock, 0, c.stream>>>(d, m[a], m[b].p, red, g_mix.st);
+    k_mix_calc_ur4<TH><<<gu, kBlock, 0, c.stream>>>(d, m[b], red, g_mix.st);
+  }
+}
+
 void mixed_release() {
   MixChunk& g = g_mix;
   if (g.graph) cudaGraphExecDestroy(g.graph);
+  if (g.graph_fused) cudaGraphExecDestroy(g.graph_fused);
   for (float*& b : g.base) {
     cudaFree(b);
     b = nullptr;
@@ -623,9 +751,9 @@ static bool mixed_alloc(Chunk& c) {
   g.S = ((long long)(c.x_max + 2 * c.H + 1 + 63) / 64) * 64;
   const long long off = (64 - (c.H % 64)) % 64;
   const size_t n = (size_t)(off + (c.y_max + 2 * c.H + 1) * g.S + 64);
-  float** f[10] = {&g.dev.Kx, &g.dev.Ky, &g.dev.D, &g.dev.Mi, &g.dev.d,
-                   &g.dev.r,  &g.dev.p,  &g.dev.w, &g.dev.z,  &g.dev.sd};
-  for (int i = 0; i < 10; i++) {
+  float** f[11] = {&g.dev.Kx, &g.dev.Ky, &g.dev.D, &g.dev.Mi, &g.dev.d, &g.dev.r,
+                   &g.dev.p,  &g.dev.w,  &g.dev.z, &g.dev.sd, &g.dev.p2};
+  for (int i = 0; i < 11; i++) {
     if (!check_cuda(cudaMalloc(&g.base[i], n * sizeof(float)), "cudaMalloc mixed field"))
       return false;
     cudaMemsetAsync(g.base[i], 0, n * sizeof(float), c.stream);
@@ -687,7 +815,7 @@ static cudaGraphExec_t mix_capture(Chunk& c, F enqueue) {
 // Uploads h, replays `graph` (iters_per_replay iterations, `kernels`
 // kernels each) until the inner loop has stopped, and reads h back.
 static bool run_inner(Chunk& c, cudaGraphExec_t graph, int iters_per_replay, int kernels,
-                      MixState& h) {
+                      MixState& h, bool stop_only = false) {
   MixChunk& g = g_mix;
   if (!check_cuda(cudaMemcpyAsync(g.st, &h, sizeof(MixState), cudaMemcpyHostToDevice,
                                   c.stream),
@@ -706,7 +834,9 @@ static bool run_inner(Chunk& c, cudaGraphExec_t graph, int iters_per_replay, int
                     "mixed state read") ||
         !check_cuda(cudaStreamSynchronize(c.stream), "mixed sync"))
       return false;
-    if (h.stop && !h.p_pending) return true;
+    // the loop with calc_p folded into calc_w leaves the last p' unformed:
+    // a CG correction starts again from p = z
+    if (h.stop && (stop_only || !h.p_pending)) return true;
   }
 }
 
@@ -726,12 +856,18 @@ static bool mixed_solve_t(Chunk& c, double tol, double inner_tol, int max_outer,
   if (g.graph && g.graph_epoch != c.field_epoch) {
     cudaGraphExecDestroy(g.graph);  // the chunk's r/sd buffers have traded places
     g.graph = nullptr;
+    if (g.graph_fused) cudaGraphExecDestroy(g.graph_fused);
+    g.graph_fused = nullptr;
   }
   if (!g.graph) {
     g.graph = mix_capture(c, [&]() { enqueue_inner<TH>(c, batch); });
     if (!g.graph) return false;
     g.graph_batch = batch;
     g.graph_epoch = c.field_epoch;
+  }
+  if (!g.graph_fused) {
+    g.graph_fused = mix_capture(c, [&]() { enqueue_inner_fused<TH>(c, batch); });
+    if (!g.graph_fused) return false;
   }
   double res[2];
   auto outer_residual = [&](double* out) -> bool {
@@ -837,7 +973,7 @@ static bool mixed_solve_t(Chunk& c, double tol, double inner_tol, int max_outer,
         if (!run_inner(c, ppcg_graph, ppcg_batch, ppcg_batch * (5 + 2 * inner_steps), h))
           return cleanup(false);
         cheby_total += (long long)h.done_iters * inner_steps;
-      } else if (!run_inner(c, g.graph, batch, 3 * batch, h)) {
+      } else if (!run_inner(c, g.graph_fused, batch, 2 * batch, h, true)) {
         return cleanup(false);
       }
       inner_total += h.done_iters;

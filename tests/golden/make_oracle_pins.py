@@ -18,6 +18,12 @@ them with these records bit for bit.  The deck text is stored with the
 record, so the pin says exactly what it pins.
 
     make_oracle_pins.py --workload ppcg4096|cheby4096 [--exact|--chain] [--cap N]
+
+Largest grid.  tests/test_gpu_large.py runs the same PPCG deck at 8192^2
+(the grid of the mixed-precision configuration) for one timestep, ended
+LARGE_CAP iterations after its switch from CG, against these records.
+
+    make_oracle_pins.py --large 8192 [--exact|--chain]
 """
 import json
 import os
@@ -33,6 +39,7 @@ from oracle import oracle  # noqa: E402
 HEADLINE_FILE = os.path.join(HERE, "oracle_pins_headline.json")
 HEADLINE_STEPS = 2
 HEADLINE_CAP = 20
+LARGE_CAP = 5
 
 
 def headline_deck(workload, form, steps=HEADLINE_STEPS):
@@ -46,9 +53,20 @@ def headline_deck(workload, form, steps=HEADLINE_STEPS):
         bench.ARITHMETIC = saved
 
 
-def pin_headline(workload, form, cap):
+def large_deck(cells, form):
+    """bench.py's ppcg4096 deck (five states, PPCG, block Jacobi, halo depth
+    2, 10 inner steps, 20 CG steps before the switch, tl_eps 1e-15,
+    tl_max_iters 1000) at cells^2, one timestep."""
+    from tealeaf_opencl_gb300 import decks
+    return decks.five_state_deck(cells, solver="ppcg", prec="jac_block", steps=1,
+                                 eps=1e-15, max_iters=1000, halo=2, inner_steps=10,
+                                 presteps=20, summary_frequency=0,
+                                 extra="tl_arithmetic %s" % form)
+
+
+def pin_headline(workload, form, cap, deck=None):
     pins = json.load(open(HEADLINE_FILE)) if os.path.exists(HEADLINE_FILE) else {}
-    deck = headline_deck(workload, form)
+    deck = deck or headline_deck(workload, form)
     t0 = time.time()
     res = oracle.run_deck(deck, max_after_switch=cap)
     n = res.n_steps
@@ -100,7 +118,10 @@ def main(tps, form):
 if __name__ == "__main__":
     args = sys.argv[1:]
     form = "fused" if "--fused" in args else "chain" if "--chain" in args else "exact"
-    if "--workload" in args:
+    if "--large" in args:
+        cells = int(args[args.index("--large") + 1])
+        pin_headline("ppcg%d" % cells, form, LARGE_CAP, large_deck(cells, form))
+    elif "--workload" in args:
         wl = args[args.index("--workload") + 1]
         cap = int(args[args.index("--cap") + 1]) if "--cap" in args else HEADLINE_CAP
         pin_headline(wl, form, cap)

@@ -1,0 +1,78 @@
+"""The largest grid of the benchmark set: 8192^2.
+
+bench.py's PPCG deck (five states, block Jacobi, halo depth 2, 10 inner
+steps, 20 CG steps before the switch, tl_eps 1e-15) at 8192^2, the grid of
+the mixed-precision configuration, for one timestep ended 5 iterations after
+its switch from CG (about 70 M cells and 11 GB of fields on the device):
+
+  * each arithmetic form matches the oracle's run of the same deck bit for
+    bit (tests/golden/oracle_pins_headline.json, ppcg8192/*, made by
+    make_oracle_pins.py --large 8192), through the device-resident driver
+    and, for the chain form, through the per-call C ABI;
+  * the chain form agrees with the exact one within 1e-11 relative in the
+    field summary and +-1 in the iteration counts (the oracle's two runs
+    differ by 2.0e-12 in ie and 1.0e-13 in temp: the step stops 5 iterations
+    after the switch at CG iteration 785, far from convergence, on an
+    operator 4 times worse conditioned than at 4096^2, where the forms agree
+    to 3.7e-14 under the 1e-12 bar of tests/test_gpu_headline.py);
+  * a second run gives the same bits.
+"""
+import json
+import os
+
+import pytest
+
+from tealeaf_opencl_gb300 import lib
+
+pytestmark = pytest.mark.gpu
+PINS = os.path.join(os.path.dirname(__file__), "golden", "oracle_pins_headline.json")
+REL_TOL = 1e-11
+ITER_TOL = 1
+
+
+def pin(form):
+    pins = json.load(open(PINS))
+    key = "ppcg8192/%s" % form
+    if key not in pins:
+        pytest.skip("no 8192^2 pin for %s" % form)
+    return pins[key]
+
+
+def run(p, mode):
+    return lib.run_deck(p["deck"], mode=mode, cap_after_switch=p["cap_after_switch"])
+
+
+def summary(step):
+    return dict(vol=step.vol, mass=step.mass, ie=step.ie, temp=step.temp)
+
+
+def check(steps, p):
+    assert [s.iterations for s in steps] == p["iterations"]
+    assert [s.inner_iterations for s in steps] == p["inner_iterations"]
+    assert [s.switch_iteration for s in steps] == p["switch_iteration"]
+    got = summary(steps[-1])
+    assert {k: float(v).hex() for k, v in got.items()} == p["summary_hex"]
+
+
+def test_largest_grid_matches_oracle_in_both_forms():
+    runs = {}
+    for form in ("exact", "chain"):
+        p = pin(form)
+        steps = run(p, lib.DRIVER_RESIDENT)
+        assert steps and all(s.switch_iteration > 0 for s in steps)
+        check(steps, p)
+        runs[form] = steps
+    ex, ch = runs["exact"][-1], runs["chain"][-1]
+    assert abs(ex.iterations - ch.iterations) <= ITER_TOL
+    se, sc = summary(ex), summary(ch)
+    assert se["vol"] == sc["vol"] and se["mass"] == sc["mass"]
+    for k in se:
+        assert abs(se[k] - sc[k]) <= REL_TOL * abs(se[k]), (k, se[k], sc[k])
+
+
+def test_largest_grid_repeats_and_per_call_path_agrees():
+    p = pin("chain")
+    first = run(p, lib.DRIVER_RESIDENT)
+    again = run(p, lib.DRIVER_RESIDENT)
+    assert [summary(s) for s in first] == [summary(s) for s in again]
+    check(run(p, lib.DRIVER_PER_CALL), p)

@@ -110,6 +110,31 @@ def test_headline_pins_are_the_bench_decks_and_forms_agree(workload):
         assert abs(x - y) <= 1e-12 * abs(x), k
 
 
+def test_largest_grid_pins_are_the_ppcg_deck_at_8192_and_forms_agree():
+    """The 8192^2 pins hold bench.py's PPCG deck at that grid (one
+    timestep), in the exact and chain forms, past the switch from CG.  On
+    the oracle the two forms take the same iterations; their field summaries
+    agree to 2.0e-12 relative (ie) and 1.0e-13 (temp).  The step ends 5
+    iterations after the switch at CG iteration 785, far from convergence,
+    and at 8192^2 the operator's condition number is 4 times that of the
+    4096^2 grid (where the forms agree to 3.7e-14), so the bar here is
+    1e-11."""
+    from tests.golden.make_oracle_pins import LARGE_CAP, large_deck
+    pins = json.load(open(HEADLINE_PINS))
+    got = {}
+    for form in ("exact", "chain"):
+        p = pins["ppcg8192/%s" % form]
+        assert p["deck"] == large_deck(8192, form)
+        assert p["cap_after_switch"] == LARGE_CAP
+        assert p["switch_iteration"][0] >= 20
+        got[form] = p
+    a, b = got["exact"], got["chain"]
+    assert all(abs(x - y) <= 1 for x, y in zip(a["iterations"], b["iterations"]))
+    for k, v in a["summary_hex"].items():
+        x, y = float.fromhex(v), float.fromhex(b["summary_hex"][k])
+        assert abs(x - y) <= 1e-11 * abs(x), k
+
+
 @pytest.mark.parametrize("solver", ["ppcg", "chebyshev"])
 def test_cap_after_switch_bounds_the_polynomial_phase(solver):
     """max_after_switch ends a step that many iterations after its switch,
