@@ -450,15 +450,21 @@ __global__ void __launch_bounds__(kBlock, 4)
 // finishes the reduction carries out the host steps of one CG iteration
 // (cg_scalar_step).  With NV = 2 it also sums r.r, for the resident loop's
 // optional exit test on the unpreconditioned residual.
+// With r.r as well (NV = 2) the restrict-qualified body needs more registers
+// than 4 blocks per SM leave (202.5 against 188.7 us at 4096^2, diagonal
+// Jacobi), so that variant keeps cg_ur_tile at 3 blocks per SM.
 template <int TH, int F, int NV = 1>
-__global__ void __launch_bounds__(kBlock, 4)
+__global__ void __launch_bounds__(kBlock, NV == 2 ? 3 : 4)
     k_cg_calc_ur(Dev d, Red red, double alpha, ResState* st) {
   if (st) {
     if (*(volatile int*)&st->stop) return;
     alpha = st->rro / st->pw;
   }
   const bool last = tile_driver<TH, NV>(d, red, [&](int x, int y0, bool xin, double* acc) {
-    cg_ur_tile_r<TH, F, NV>(d, x, y0, xin, acc, alpha);
+    if constexpr (NV == 2)
+      cg_ur_tile<TH, F, NV>(d, x, y0, xin, acc, alpha);
+    else
+      cg_ur_tile_r<TH, F, NV>(d, x, y0, xin, acc, alpha);
   });
   if (st && last && threadIdx.x == 0) {
     cg_scalar_step<NV>(st, alpha, red.result);
