@@ -43,6 +43,7 @@ import subprocess
 import sys
 import threading
 import time
+from pathlib import Path
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -234,7 +235,7 @@ class Clocks:
 def measured_peak_hbm():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
-        return float(json.load(open(path))["hbm_gbs"]), "measured"
+        return float(json.loads(Path(path).read_text())["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return 6800.0, "fallback"
 
@@ -243,7 +244,7 @@ def ncu_traffic(kernel, workload):
     """DRAM bytes per launch of the kernel from a committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
-        return json.load(open(path))[workload][kernel]["dram_bytes_per_launch"]
+        return json.loads(Path(path).read_text())[workload][kernel]["dram_bytes_per_launch"]
     except (OSError, KeyError, ValueError):
         return None
 

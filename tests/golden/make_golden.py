@@ -14,6 +14,7 @@ import json
 import os
 import re
 import sys
+from pathlib import Path
 
 REF = None  # the reference tree, from the command line
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -24,13 +25,13 @@ DECKS = {2: "tea_bm_short.in", 3: "tea_bm16_short.in", 4: "tea_bm.in",
 
 def default_deck():
     """The deck initialise.f90 writes when no tea.in exists (test problem 1)."""
-    src = open(os.path.join(REF, "initialise.f90")).read()
+    src = Path(os.path.join(REF, "initialise.f90")).read_text()
     lines = re.findall(r"WRITE\(out_unit,'\(A\)'\)'(.*)'", src)
     return "\n".join(lines) + "\n"
 
 
 def goldens():
-    src = open(os.path.join(REF, "field_summary.f90")).read()
+    src = Path(os.path.join(REF, "field_summary.f90")).read_text()
     out = {}
     for tp, val in re.findall(
             r"IF\(test_problem\.EQ\.(\d)\) qa_diff=ABS\(\(100\.0_8\*\(temp/([0-9.]+)_8\)\)", src):
@@ -47,7 +48,7 @@ def main():
         f.write(default_deck())
     meta["problems"]["1"] = {"deck": "tp1.in", "temp": g[1]}
     for tp, name in DECKS.items():
-        text = open(os.path.join(REF, name)).read()
+        text = Path(os.path.join(REF, name)).read_text()
         out = "tp%d.in" % tp
         with open(os.path.join(HERE, out), "w") as f:
             f.write(text)

@@ -29,6 +29,7 @@ import json
 import os
 import sys
 import time
+from pathlib import Path
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
@@ -65,7 +66,7 @@ def large_deck(cells, form):
 
 
 def pin_headline(workload, form, cap, deck=None):
-    pins = json.load(open(HEADLINE_FILE)) if os.path.exists(HEADLINE_FILE) else {}
+    pins = json.loads(Path(HEADLINE_FILE).read_text()) if os.path.exists(HEADLINE_FILE) else {}
     deck = deck or headline_deck(workload, form)
     t0 = time.time()
     res = oracle.run_deck(deck, max_after_switch=cap)
@@ -84,7 +85,7 @@ def pin_headline(workload, form, cap, deck=None):
         "oracle_threads": oracle.lib().oracle_num_threads(),
         "oracle_seconds": round(time.time() - t0, 1),
     }
-    json.dump(pins, open(HEADLINE_FILE, "w"), indent=1, sort_keys=True)
+    Path(HEADLINE_FILE).write_text(json.dumps(pins, indent=1, sort_keys=True))
     print(workload, form, list(res.iterations[:n]), list(res.switch_iteration[:n]),
           final[5], flush=True)
 
@@ -92,11 +93,11 @@ def pin_headline(workload, form, cap, deck=None):
 def main(tps, form):
     path = os.path.join(HERE, "oracle_pins.json" if form == "exact"
                         else "oracle_pins_%s.json" % form)
-    pins = json.load(open(path)) if os.path.exists(path) else {}
-    meta = json.load(open(os.path.join(HERE, "test_problems.json")))
+    pins = json.loads(Path(path).read_text()) if os.path.exists(path) else {}
+    meta = json.loads(Path(os.path.join(HERE, "test_problems.json")).read_text())
     for tp in tps:
         p = meta["problems"][str(tp)]
-        deck = open(os.path.join(HERE, p["deck"])).read()
+        deck = Path(os.path.join(HERE, p["deck"])).read_text()
         deck = deck.replace("*endtea", "tl_arithmetic %s\n*endtea" % form, 1)
         t0 = time.time()
         res = oracle.run_deck(deck)
@@ -111,7 +112,7 @@ def main(tps, form):
             "oracle_threads": oracle.lib().oracle_num_threads(),
             "oracle_seconds": round(time.time() - t0, 1),
         }
-        json.dump(pins, open(path, "w"), indent=1, sort_keys=True)
+        Path(path).write_text(json.dumps(pins, indent=1, sort_keys=True))
         print(tp, res.final_temp, res.qa_diff, flush=True)
 
 

@@ -5,6 +5,7 @@ No compute call is made: this runs without a GPU.
 import ctypes
 import os
 import re
+from pathlib import Path
 
 from oracle import oracle
 from tealeaf_opencl_gb300 import lib
@@ -14,7 +15,7 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(__file__)), "include",
 
 
 def declared():
-    text = open(HEADER).read()
+    text = Path(HEADER).read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return re.findall(r"^[a-z][\w *]*?[\s*](\w+)\s*\(", text, flags=re.M)
 

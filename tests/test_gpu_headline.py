@@ -16,6 +16,7 @@ its switch from CG (the first step switches at CG iteration 361), and
 """
 import json
 import os
+from pathlib import Path
 
 import pytest
 
@@ -28,7 +29,7 @@ ITER_TOL = 1     # iteration counts
 
 
 def pin(workload, form):
-    return json.load(open(PINS))["%s/%s" % (workload, form)]
+    return json.loads(Path(PINS).read_text())["%s/%s" % (workload, form)]
 
 
 def run(p, mode):

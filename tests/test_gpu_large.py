@@ -19,6 +19,7 @@ its switch from CG (about 70 M cells and 11 GB of fields on the device):
 """
 import json
 import os
+from pathlib import Path
 
 import pytest
 
@@ -31,7 +32,7 @@ ITER_TOL = 1
 
 
 def pin(form):
-    pins = json.load(open(PINS))
+    pins = json.loads(Path(PINS).read_text())
     key = "ppcg8192/%s" % form
     if key not in pins:
         pytest.skip("no 8192^2 pin for %s" % form)

@@ -14,6 +14,7 @@ calls)', with nonzero totals.
 import json
 import os
 import re
+from pathlib import Path
 
 import pytest
 
@@ -32,11 +33,11 @@ def fortran_float(s):
 
 
 def test_problem_1_log_has_the_reference_layout(tmp_path):
-    meta = json.load(open(os.path.join(GOLD, "test_problems.json")))
-    deck = open(os.path.join(GOLD, meta["problems"]["1"]["deck"])).read()
+    meta = json.loads(Path(os.path.join(GOLD, "test_problems.json")).read_text())
+    deck = Path(os.path.join(GOLD, meta["problems"]["1"]["deck"])).read_text()
     log = str(tmp_path / "tea.out")
     steps = lib.run_deck(deck, log_path=log)
-    text = open(log).read().splitlines()
+    text = Path(log).read_text().splitlines()
     # the first summary (start.f90) and the last (diffuse.f90's final call)
     step_lines = [ln for ln in text if ln.startswith(" step:")]
     assert len(step_lines) >= 2
@@ -70,7 +71,7 @@ def test_ppcg_log_reports_the_switch_in_the_reference_layout(tmp_path):
                                  halo=2, inner_steps=8, presteps=20)
     log = str(tmp_path / "tea.out")
     steps = lib.run_deck(deck, log_path=log)
-    text = open(log).read().splitlines()
+    text = Path(log).read_text().splitlines()
     sw = [ln for ln in text if ln.startswith("Switching after")]
     assert len(sw) == 2
     # '(a,i3,a,e15.7)': "Switching after ", i3, " CG its, error ", e15.7

@@ -8,6 +8,7 @@ count in every timestep and the same field_summary values.
 """
 import json
 import os
+from pathlib import Path
 
 import pytest
 
@@ -19,15 +20,15 @@ GOLD = os.path.join(os.path.dirname(__file__), "golden")
 
 
 def problem(tp):
-    meta = json.load(open(os.path.join(GOLD, "test_problems.json")))
+    meta = json.loads(Path(os.path.join(GOLD, "test_problems.json")).read_text())
     p = meta["problems"][str(tp)]
-    return open(os.path.join(GOLD, p["deck"])).read(), p["temp"]
+    return Path(os.path.join(GOLD, p["deck"])).read_text(), p["temp"]
 
 
 def pins(mode):
     name = "oracle_pins.json" if mode == "exact" else "oracle_pins_%s.json" % mode
     path = os.path.join(GOLD, name)
-    return json.load(open(path)) if os.path.exists(path) else {}
+    return json.loads(Path(path).read_text()) if os.path.exists(path) else {}
 
 
 def with_arithmetic(deck, mode):

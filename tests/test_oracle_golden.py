@@ -7,6 +7,7 @@ from the reference tree by tests/golden/make_golden.py.
 """
 import json
 import os
+from pathlib import Path
 
 import pytest
 
@@ -16,9 +17,9 @@ GOLD = os.path.join(os.path.dirname(__file__), "golden")
 
 
 def problem(tp):
-    meta = json.load(open(os.path.join(GOLD, "test_problems.json")))
+    meta = json.loads(Path(os.path.join(GOLD, "test_problems.json")).read_text())
     p = meta["problems"][str(tp)]
-    return open(os.path.join(GOLD, p["deck"])).read(), p["temp"]
+    return Path(os.path.join(GOLD, p["deck"])).read_text(), p["temp"]
 
 
 def check(tp, mode="fused"):
@@ -90,7 +91,7 @@ def test_headline_pins_are_the_bench_decks_and_forms_agree(workload):
     and chain forms; on the oracle the two forms agree to 1e-12 in the
     field summary and to 1 in every iteration count."""
     import bench
-    pins = json.load(open(HEADLINE_PINS))
+    pins = json.loads(Path(HEADLINE_PINS).read_text())
     got = {}
     for form in ("exact", "chain"):
         p = pins["%s/%s" % (workload, form)]
@@ -120,7 +121,7 @@ def test_largest_grid_pins_are_the_ppcg_deck_at_8192_and_forms_agree():
     4096^2 grid (where the forms agree to 3.7e-14), so the bar here is
     1e-11."""
     from tests.golden.make_oracle_pins import LARGE_CAP, large_deck
-    pins = json.load(open(HEADLINE_PINS))
+    pins = json.loads(Path(HEADLINE_PINS).read_text())
     got = {}
     for form in ("exact", "chain"):
         p = pins["ppcg8192/%s" % form]
