@@ -24,6 +24,13 @@ Largest grid.  tests/test_gpu_large.py runs the same PPCG deck at 8192^2
 LARGE_CAP iterations after its switch from CG, against these records.
 
     make_oracle_pins.py --large 8192 [--exact|--chain]
+
+Mixed precision with 16-row reduction tiles.  tests/test_gpu_mixed.py runs
+the FP32-inner / FP64-corrected CG solve at 2048x2440 (the smallest grid
+with 16-row tiles) for one timestep to a 1e-8 relative residual against
+this record.
+
+    make_oracle_pins.py --mixed-tall
 """
 import json
 import os
@@ -63,6 +70,37 @@ def large_deck(cells, form):
                                  eps=1e-15, max_iters=1000, halo=2, inner_steps=10,
                                  presteps=20, summary_frequency=0,
                                  extra="tl_arithmetic %s" % form)
+
+
+def mixed_tall_deck():
+    """Mixed precision (FP32 inner CG, diagonal Jacobi) at 2048x2440, one
+    timestep to 1e-8, inner tolerance 1e-4."""
+    from tealeaf_opencl_gb300 import decks
+    return decks.five_state_deck(2048, solver="cg", prec="jac_diag", steps=1, eps=1e-8,
+                                 max_iters=20000, y_cells=2440,
+                                 extra="tl_mixed_precision\ntl_mixed_inner_eps 1e-4\n")
+
+
+def pin_mixed_tall():
+    pins = json.loads(Path(HEADLINE_FILE).read_text()) if os.path.exists(HEADLINE_FILE) else {}
+    deck = mixed_tall_deck()
+    t0 = time.time()
+    res = oracle.run_deck(deck)
+    n = res.n_steps
+    final = res.summaries()[-1]
+    pins["mixed2048x2440"] = {
+        "deck": deck,
+        "iterations": list(res.iterations[:n]),
+        "outer_corrections": list(res.outer_corrections[:n]),
+        "relative_residual_hex": [float(v).hex() for v in res.relative_residual[:n]],
+        "summary_hex": {k: float(final[i]).hex()
+                        for k, i in (("vol", 1), ("mass", 2), ("ie", 4), ("temp", 5))},
+        "oracle_threads": oracle.lib().oracle_num_threads(),
+        "oracle_seconds": round(time.time() - t0, 1),
+    }
+    Path(HEADLINE_FILE).write_text(json.dumps(pins, indent=1, sort_keys=True))
+    print("mixed2048x2440", list(res.iterations[:n]), list(res.outer_corrections[:n]),
+          list(res.relative_residual[:n]), flush=True)
 
 
 def pin_headline(workload, form, cap, deck=None):
@@ -119,7 +157,9 @@ def main(tps, form):
 if __name__ == "__main__":
     args = sys.argv[1:]
     form = "fused" if "--fused" in args else "chain" if "--chain" in args else "exact"
-    if "--large" in args:
+    if "--mixed-tall" in args:
+        pin_mixed_tall()
+    elif "--large" in args:
         cells = int(args[args.index("--large") + 1])
         pin_headline("ppcg%d" % cells, form, LARGE_CAP, large_deck(cells, form))
     elif "--workload" in args:

@@ -40,6 +40,29 @@ def test_mixed_matches_oracle(cells, y_cells, inner):
     assert all(s.relative_residual <= 1e-10 for s in steps)
 
 
+def test_mixed_tall_tiles_match_oracle_pin():
+    """2048x2440, the smallest grid with 16-row reduction tiles, one
+    timestep to 1e-8: iteration counts, corrections, residual and field
+    summary bit for bit against the oracle's run of the same deck
+    (tests/golden/oracle_pins_headline.json, made by make_oracle_pins.py
+    --mixed-tall; the oracle needs minutes for it)."""
+    import json
+    import os
+    from pathlib import Path
+    path = os.path.join(os.path.dirname(__file__), "golden", "oracle_pins_headline.json")
+    p = json.loads(Path(path).read_text()).get("mixed2048x2440")
+    if p is None:
+        pytest.skip("no mixed 2048x2440 pin")
+    assert lib.load().tea_gb300_reduction_rows(2048, 2440) == 16
+    steps = lib.run_deck(p["deck"])
+    assert [s.iterations for s in steps] == p["iterations"]
+    assert [s.outer_corrections for s in steps] == p["outer_corrections"]
+    assert [float(s.relative_residual).hex() for s in steps] == p["relative_residual_hex"]
+    last = steps[-1]
+    got = dict(vol=last.vol, mass=last.mass, ie=last.ie, temp=last.temp)
+    assert {k: float(v).hex() for k, v in got.items()} == p["summary_hex"]
+
+
 def test_mixed_answer_agrees_with_fp64():
     """Both solves stop at a true relative residual of 1e-10."""
     cells = 512

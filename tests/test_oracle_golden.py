@@ -136,6 +136,16 @@ def test_largest_grid_pins_are_the_ppcg_deck_at_8192_and_forms_agree():
         assert abs(x - y) <= 1e-11 * abs(x), k
 
 
+def test_mixed_tall_pin_is_its_deck():
+    """The mixed-precision pin at 2048x2440 holds the deck
+    make_oracle_pins.py builds for it, and its solve reached 1e-8."""
+    from tests.golden.make_oracle_pins import mixed_tall_deck
+    p = json.loads(Path(HEADLINE_PINS).read_text())["mixed2048x2440"]
+    assert p["deck"] == mixed_tall_deck()
+    assert all(float.fromhex(v) <= 1e-8 for v in p["relative_residual_hex"])
+    assert all(c >= 1 for c in p["outer_corrections"])
+
+
 @pytest.mark.parametrize("solver", ["ppcg", "chebyshev"])
 def test_cap_after_switch_bounds_the_polynomial_phase(solver):
     """max_after_switch ends a step that many iterations after its switch,
