@@ -167,6 +167,25 @@ class Dist:
             self.pg.destroy_process_group()
 
 
+def step_bytes_per_cell_iteration(name):
+    """Algorithmic HBM bytes per cell-iteration of a whole solver iteration:
+    the fields the reference's kernels read and write, each once
+    (KERNEL_BYTES), summed over the kernels of one iteration and divided by
+    the cell-iterations it counts (PPCG: one outer plus its inner steps)."""
+    cells, solver, prec, halo, inner = WORKLOADS[name][:5]
+    kb = lambda k: KERNEL_BYTES[k][prec] if isinstance(KERNEL_BYTES[k], dict) else KERNEL_BYTES[k]
+    cg = kb("tea_leaf_cg_solve_calc_w") + kb("tea_leaf_cg_solve_calc_ur") + \
+        kb("tea_leaf_cg_solve_calc_p")
+    if solver == "cg":
+        return cg
+    if solver == "chebyshev":
+        return kb("tea_leaf_cheby_solve_calc_p") + kb("tea_leaf_cheby_solve_calc_u")
+    # PPCG: calc_w, calc_ur, init_sd, the inner steps, r.z, calc_p
+    outer = cg + kb("tea_leaf_ppcg_solve_init_sd") + kb("tea_leaf_calc_2norm") + inner * (
+        kb("tea_leaf_ppcg_solve_update_r") + kb("tea_leaf_ppcg_solve_calc_sd"))
+    return outer / (1 + inner)
+
+
 def whole_job_rate(dist, cell_iters, seconds):
     """Cell-iterations per second of the whole job: every rank's count
     summed, over the slowest rank's time (replicas run the same work)."""
@@ -380,6 +399,14 @@ def run_ours(args, dist):
                      "fp64_pipe": fp64},
         "clocks": clk,
     }
+    bpc = step_bytes_per_cell_iteration(name)
+    out["step_hbm"] = {
+        "algorithmic_bytes_per_cell_iteration": bpc,
+        "gbs": value * bpc / 1e9, "peak": peak,
+        "frac": value * bpc / 1e9 / peak if peak else None,
+        "unit": "GB/s",
+        "basis": "the reference kernels' fields per solver iteration, each once, "
+                 "over the resident timed region"}
     return out
 
 
