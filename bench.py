@@ -52,7 +52,7 @@ WORKLOADS = {
     # name: (cells, solver, prec, halo, inner, presteps, eps, dominant kernel,
     #        algorithmic bytes per cell of one launch of it)
     "ppcg4096": (4096, "ppcg", "jac_block", 2, 10, 20, 1e-15,
-                 "tea_leaf_ppcg_solve_update_r", 56),
+                 "tea_leaf_ppcg_solve_inner_step", 112),
     "cheby4096": (4096, "chebyshev", "jac_block", 2, 10, 20, 1e-15,
                   "tea_leaf_cheby_solve_calc_p_u", 104),
     "cg4096": (4096, "cg", "jac_block", 2, 10, 20, 1e-15,
@@ -76,6 +76,9 @@ FP64_PER_CELL = {
     # two inner steps of update_r + calc_sd (6 + 2.5 each in the fused forms)
     ("tea_leaf_ppcg_solve_inner_pair", "jac_block", "chain"): 17,
     ("tea_leaf_ppcg_solve_inner_pair", "jac_block", "fused"): 17,
+    # one inner step in one pass: update_r 6 + calc_sd 3.5
+    ("tea_leaf_ppcg_solve_inner_step", "jac_block", "chain"): 9.5,
+    ("tea_leaf_ppcg_solve_inner_step", "jac_block", "fused"): 9.5,
     ("tea_leaf_ppcg_solve_update_r", "jac_block", "chain"): 6,
     ("tea_leaf_ppcg_solve_update_r", "jac_block", "fused"): 6,
     ("tea_leaf_ppcg_solve_update_r", "jac_block", "exact"): 9,
@@ -418,6 +421,8 @@ KERNEL_BYTES = {
     "tea_leaf_cg_solve_calc_p": 24,       # r z p, w p
     "tea_leaf_calc_2norm": 16,
     "tea_leaf_ppcg_solve_update_r": 56,   # r u r Kx Ky sd, w u r
+    # update_r and calc_sd in one pass (block Jacobi): the two kernels' fields
+    "tea_leaf_ppcg_solve_inner_step": {"jac_diag": 88, "jac_block": 112, "none": 80},
     "tea_leaf_ppcg_solve_inner_pair": 88,  # two steps: r u r sd Kx Ky diag cp bfp, w u r sd
     "tea_leaf_ppcg_solve_calc_sd": {"jac_diag": 32, "jac_block": 56, "none": 24},
     "tea_leaf_cheby_solve_calc_p": {"jac_diag": 80, "jac_block": 96, "none": 72},
@@ -904,7 +909,7 @@ def main():
                          "from the switch from CG on")
     ap.add_argument("--inner-pairs", type=int, default=0, choices=[0, 1],
                     help="PPCG inner steps two at a time in one TMA-fed pass (1) or one "
-                         "update_r + calc_sd launch pair per step (0, the faster on GB300)")
+                         "one-pass update_r + calc_sd per step (0, the faster on GB300)")
     ap.add_argument("--no-other-workloads", action="store_true",
                     help="leave out the compact cg512 / cheby4096 / batch / adjoint measurements "
                          "of the default line")

@@ -818,6 +818,15 @@ extern "C" void tea_leaf_ppcg_inner_kernel_ocl_(int* inner_step,
     }
   }
   flush_pending_inner(c);
+  if (c.prec == PREC_JAC_BLOCK) {
+    // update_r and calc_sd in one pass (k_ppcg_step): the new sd goes to
+    // the second buffer, which then becomes sd
+    if (!ensure_alt_fields(c)) return;
+    launch_ppcg_step(c, c.ppcg_alpha_h[s], c.ppcg_beta_h[s], c.sd.f, c.sd2.f);
+    std::swap(c.sd, c.sd2);
+    c.field_epoch++;
+    return;
+  }
   launch_ppcg_update_r(c);
   launch_ppcg_calc_sd(c, c.ppcg_alpha_h[s], c.ppcg_beta_h[s]);
 }

@@ -206,6 +206,9 @@ void launch_cheby_calc_u(Chunk& c);
 void launch_cheby_calc_pu(Chunk& c, double alpha, double beta, double* un);
 void launch_ppcg_init_sd(Chunk& c, double theta);
 void launch_ppcg_update_r(Chunk& c);
+// update_r and calc_sd of one inner step in one pass (block Jacobi), sd
+// read from sdi and the new sd written to sdo
+void launch_ppcg_step(Chunk& c, double alpha, double beta, const double* sdi, double* sdo);
 void launch_ppcg_calc_sd(Chunk& c, double alpha, double beta);
 void launch_jacobi_copy_u(Chunk& c);
 void launch_jacobi_solve(Chunk& c);

@@ -846,6 +846,90 @@ __global__ void __launch_bounds__(kBlock, kSdMinBlocks)
   }
 }
 
+// One PPCG inner step with the block-Jacobi preconditioner in one pass:
+// tea_leaf_ppcg_solve_update_r (tea_leaf_ppcg_cl.cl:62-88) and then
+// tea_leaf_ppcg_solve_calc_sd (:90-134) on the r it has just formed.  A lane
+// takes one column of one 4-row strip: u += sd and r -= A sd at its 4
+// cells, then z = M^-1 r by the strip's sweep (the rows' Ky shared with the
+// operator) and sd' = alpha sd + beta z.  Other blocks still read this
+// block's sd for their operator, so sd' goes to sdo; u and r are read only
+// at their own cells and are updated in place.  The arithmetic is that of
+// the two kernels (bit-identical); 9.5 FP64 instructions and 112 algorithmic
+// bytes per cell against 6 + 3.5 and 56 + 56 for the two passes.  At 4096^2
+// on non-zero fields 302-305 us against 322.4 us for update_r + calc_sd, at
+// 3 blocks per SM (80 registers; 4 blocks per SM with 64 registers 317-321
+// us).
+template <int F>
+__global__ void __launch_bounds__(kBlock, 3)
+    k_ppcg_step(Dev d, Red red, double alpha, double beta, const ResState* st,
+                const double* sdi_, double* sdo_) {
+  if (st && *(volatile const int*)&st->stop) return;
+  tile_driver<4, 0>(d, red, [&](int x, int y0, bool xin, double* acc) {
+    if (!xin) return;
+    const double* __restrict__ sdi = sdi_;
+    double* __restrict__ sdo = sdo_;
+    const double* __restrict__ kx = d.Kx;
+    const double* __restrict__ ky = d.Ky;
+    const double* __restrict__ dg = d.diag;
+    double* __restrict__ u = d.u;
+    double* __restrict__ r = d.r;
+    const long long S = d.S;
+    const long long c0 = cidx(d, x, y0);
+    const int upper = strip_rows(d, y0);
+    if (upper == 4 && y0 + 3 < d.y_max) {
+      const double* __restrict__ bfp = d.bfp;
+      const double* __restrict__ cp = d.cp;
+      double sv[6], kyv[5], rv[4], uv[4], bl[4], cl[4], z[4];
+#pragma unroll
+      for (int i = 0; i < 6; i++) sv[i] = sdi[c0 + (i - 1) * S];
+#pragma unroll
+      for (int i = 0; i < 5; i++) kyv[i] = __ldg(ky + c0 + i * S);
+      const double d0 = __ldg(dg + c0);
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const long long c = c0 + j * S;
+        uv[j] = u[c] + sv[j + 1];
+        rv[j] = bms_v<F>(r[c], j ? __ldg(dg + c) : d0, kyv[j + 1], kyv[j], __ldg(kx + c + 1),
+                         __ldg(kx + c), sv[j + 1], sv[j + 2], sv[j], sdi[c + 1], sdi[c - 1]);
+        bl[j] = __ldg(bfp + c);
+        cl[j] = j < 3 ? __ldg(cp + c) : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        u[c0 + j * S] = uv[j];
+        r[c0 + j * S] = rv[j];
+      }
+      const double kl[4] = {0.0, kyv[1], kyv[2], kyv[3]};
+      strip_solve_v<F, false, true>(4, rv, bl, kl, cl, d0, z);
+#pragma unroll
+      for (int j = 0; j < 4; j++) sdo[c0 + j * S] = sd_update<F>(alpha, sv[j + 1], beta, z[j]);
+    } else {
+      // a strip cut by the top of the interior: the two kernels' steps
+      bool in[4];
+      double sv[4], rv[4], zl[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        in[j] = y0 + j < d.y_max;
+        sv[j] = rv[j] = 0.0;
+        if (in[j]) {
+          const long long c = c0 + j * S;
+          sv[j] = sdi[c];
+          const double uv = u[c] + sv[j];
+          rv[j] = bms_v<F>(r[c], __ldg(dg + c), __ldg(ky + c + S), __ldg(ky + c),
+                           __ldg(kx + c + 1), __ldg(kx + c), sv[j], sdi[c + S], sdi[c - S],
+                           sdi[c + 1], sdi[c - 1]);
+          u[c] = uv;
+          r[c] = rv[j];
+        }
+      }
+      strip_solve<F>(d, c0, upper, rv, zl);
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (in[j]) sdo[c0 + j * S] = sd_update<F>(alpha, sv[j], beta, zl[j]);
+    }
+  });
+}
+
 // tea_leaf_ppcg_solve_update_r, tea_leaf_ppcg_cl.cl:62-88
 template <int TH, int F>
 __global__ void __launch_bounds__(kBlock, 1)
@@ -1118,6 +1202,18 @@ void launch_cheby_calc_u(Chunk& c) {
 void launch_ppcg_init_sd(Chunk& c, double theta) {
   TH4_DISPATCH(c, "tea_leaf_ppcg_solve_init_sd", k_ppcg_sd, dev4(c), c.red(), 0,
               div_const(theta), 0.0, 0.0, (const ResState*)nullptr);
+}
+
+void launch_ppcg_step(Chunk& c, double alpha, double beta, const double* sdi, double* sdo) {
+  const Dev d4 = dev4(c);
+  const char* name = "tea_leaf_ppcg_solve_inner_step";
+  const ResState* st = nullptr;
+  if (c.arith == 2)
+    launch_tile_ns(c, name, d4.ns, k_ppcg_step<2>, d4, c.red(), alpha, beta, st, sdi, sdo);
+  else if (c.arith == 1)
+    launch_tile_ns(c, name, d4.ns, k_ppcg_step<1>, d4, c.red(), alpha, beta, st, sdi, sdo);
+  else
+    launch_tile_ns(c, name, d4.ns, k_ppcg_step<0>, d4, c.red(), alpha, beta, st, sdi, sdo);
 }
 
 void launch_ppcg_update_r(Chunk& c) {
@@ -1468,12 +1564,26 @@ static void enqueue_ppcg_iterations_t(Chunk& c, int iters) {
   const bool blk = c.prec == PREC_JAC_BLOCK;
   const int gs = blk ? tile_grid(c, k_ppcg_calc_sd_block<F>, sd_blocks(d4))
                      : tile_grid(c, k_ppcg_sd<4, F>, d4.ns);
+  const int gst = tile_grid(c, k_ppcg_step<F>, d4.ns);
+  // block Jacobi: inner steps two at a time through k_ppcg_step, the first
+  // writing sd to the second buffer and the second back, so each outer
+  // iteration ends with sd where it began
+  double* const sd_a = d4.sd;
+  double* const sd_b = c.sd2.f;
   const int gz = tile_grid(c, k_ppcg_rz_step<TH, F>);
   const int gp = tile_grid(c, k_cg_calc_p<4, F>, d4.ns);
   for (int i = 0; i < iters; i++) {
     k_cg_calc_w<TH, F><<<gw, kBlock, 0, c.stream>>>(d, red, st);
     k_ppcg_ur_sd<TH, F><<<gu, kBlock, 0, c.stream>>>(d, red, st, theta);
     for (int k = 0; k < c.n_ppcg; k++) {
+      if (blk && sd_b && k + 1 < c.n_ppcg) {
+        k_ppcg_step<F><<<gst, kBlock, 0, c.stream>>>(d4, red, c.ppcg_alpha_h[k],
+                                                     c.ppcg_beta_h[k], st, sd_a, sd_b);
+        k_ppcg_step<F><<<gst, kBlock, 0, c.stream>>>(d4, red, c.ppcg_alpha_h[k + 1],
+                                                     c.ppcg_beta_h[k + 1], st, sd_b, sd_a);
+        k++;
+        continue;
+      }
       k_ppcg_update_r<4, F><<<gr, kBlock, 0, c.stream>>>(d4, red, st);
       if (blk)
         k_ppcg_calc_sd_block<F><<<gs, kBlock, 0, c.stream>>>(
@@ -1732,6 +1842,8 @@ int resident_ppcg_iterations(int n_begin, int loop_max, double rro_in,
   flush_pending_inner(c);
   const bool pairs = resident_pairs(c);
   if (pairs && (!ensure_alt_fields(c) || !tb_prepare(c))) return -1;
+  // the one-pass inner steps (k_ppcg_step) write sd to the second buffer
+  if (c.prec == PREC_JAC_BLOCK && !ensure_alt_fields(c)) return -1;
   std::vector<double> key = {c.ppcg_theta, (double)c.arith, (double)c.n_ppcg,
                              (double)c.field_epoch, pairs ? 1.0 : 0.0};
   key.insert(key.end(), c.ppcg_alpha_h, c.ppcg_alpha_h + c.n_ppcg);
@@ -1763,8 +1875,9 @@ int resident_ppcg_iterations(int n_begin, int loop_max, double rro_in,
     cudaGraphDestroy(graph);
     c.res_ppcg_key = key;
   }
-  const int per_iter =
-      pairs ? 4 + c.n_ppcg / 2 + 2 * (c.n_ppcg % 2) : 4 + 2 * c.n_ppcg;
+  const int per_iter = pairs ? 4 + c.n_ppcg / 2 + 2 * (c.n_ppcg % 2)
+                       : c.prec == PREC_JAC_BLOCK ? 4 + c.n_ppcg + c.n_ppcg % 2
+                                                  : 4 + 2 * c.n_ppcg;
   const long long max_batches = (long long)(loop_max - n_begin) / batch + 3;
   for (long long nb = 0;; nb++) {
     if (nb >= max_batches) {
