@@ -219,8 +219,8 @@ int tea_gb300_set_resident_mode(int mode);
 int tea_gb300_get_arithmetic(void);
 /* With the block-Jacobi preconditioner, PPCG inner steps can run two at a
  * time in one pass whose inputs are staged in shared memory by TMA (1), or
- * as one update_r + calc_sd pair of launches per step (0, default: on GB300
- * the pair of launches measured faster, 648 against 864 us per two steps at
+ * one step per pass, update_r and then calc_sd on the r it has formed (0,
+ * default: on GB300 measured faster, 586 against 818 us per two steps at
  * 4096^2).  With 1, tea_leaf_ppcg_inner_kernel_ocl_ holds back a step that a
  * next step may follow until that step (or any other call) arrives.
  * Results are identical either way.  Applies to the current chunk and later

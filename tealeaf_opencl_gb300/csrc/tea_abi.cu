@@ -260,7 +260,7 @@ struct Config {
   int resident_mode = 0;
   long long barrier_spin_limit = 1LL << 26;  // persistent loop's grid barrier
   int barrier_extra = 0;
-  int inner_pairs = 0;  // measured slower than the two kernels on GB300 (tea_ppcg_tb.cu)
+  int inner_pairs = 0;  // measured slower than one-pass steps on GB300 (tea_ppcg_tb.cu)
 };
 static Config g_config;
 
