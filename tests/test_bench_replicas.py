@@ -62,3 +62,20 @@ def test_single_process_needs_no_process_group():
     d = Solo()
     assert d.max(2.5) == 2.5 and d.sum(7.0) == 7.0
     assert bench.whole_job_rate(d, 100.0, 4.0) == 25.0
+
+
+def test_step_bytes_follow_the_reference_kernels():
+    """step_hbm's bytes per cell-iteration: the reference kernels' fields of
+    one solver iteration, each once (PPCG: calc_w 32, calc_ur 88, init_sd
+    48, ten inner steps of update_r 56 and calc_sd 56, r.z 16, calc_p 24,
+    over 11 cell-iterations)."""
+    import bench
+    assert bench.step_bytes_per_cell_iteration("ppcg4096") == (32 + 88 + 48 + 16 + 24 +
+                                                              10 * (56 + 56)) / 11
+    assert bench.step_bytes_per_cell_iteration("cg4096") == 32 + 88 + 24
+    assert bench.step_bytes_per_cell_iteration("cg512") == 32 + 64 + 24
+    assert bench.step_bytes_per_cell_iteration("cheby4096") == 96 + 24
+    # the one-pass inner step counts both reference kernels' fields
+    kb = bench.KERNEL_BYTES
+    assert kb["tea_leaf_ppcg_solve_inner_step"]["jac_block"] == \
+        kb["tea_leaf_ppcg_solve_update_r"] + kb["tea_leaf_ppcg_solve_calc_sd"]["jac_block"]
