@@ -1,4 +1,5 @@
-"""bench.py's replica mode on CPU: two gloo ranks.
+"""bench.py's host logic on CPU: the replica mode on two gloo ranks, and
+the whole-step byte count of its step_hbm figure.
 
 Under torchrun every rank solves its own copy of the workload and nothing is
 exchanged on the data path; the host only takes the maximum time and the sum
