@@ -513,20 +513,20 @@ __device__ __forceinline__ double cheby_update(double a, double p, double bl,
   return F ? __fma_rn(a, p, bl * br) : a * p + bl * br;
 }
 
-// tea_leaf_cheby_solve_calc_p with the block-Jacobi preconditioner alone
-// (tea_leaf_cheby_cl.cl:78-145): k_cheby_p's mode-1 block path with no
-// other path compiled in: 72 registers against 80, 340 -> 326 us at 4096^2.
-// The product beta z runs on the integer pipes (tea_emu.cuh, bit-identical):
-// on non-zero fields 340.2 -> 315.6 us.  The operator's first product there
-// as well was slower (367.0 us), and so were the sweep's multiplies by bfp
-// (388 us), which sit on each strip's dependent chain.
-// With U it also carries out tea_leaf_cheby_solve_calc_u (u = u + p,
-// tea_leaf_cheby_cl.cl:66-76) on the p it has just formed, writing the new
-// u to un: other blocks still read this block's u for their operator, so u
-// cannot be updated in place.  un then becomes u; the kernel also copies
-// u's halo ring to un, so un is exactly the in-place result.  One FP64 add
-// per cell more in this FP64-bound kernel against a separate pass over u
-// and p: 373.6 -> 350.6 us per iteration at 4096^2 (non-zero fields).
+// One Chebyshev iteration with the block-Jacobi preconditioner alone, in
+// one pass: tea_leaf_cheby_solve_calc_p (tea_leaf_cheby_cl.cl:78-145) and
+// then tea_leaf_cheby_solve_calc_u (u = u + p, :66-76) on the p it has just
+// formed.  Only this path compiled in (k_cheby_p's mode-1 block path alone
+// took 72 registers against 80, 340 -> 326 us at 4096^2).  The product
+// beta z runs on the integer pipes (tea_emu.cuh, bit-identical): on non-zero
+// fields 340.2 -> 315.6 us; the operator's first product there as well was
+// slower (367.0 us), and so were the sweep's multiplies by bfp (388 us),
+// which sit on each strip's dependent chain.  The new u goes to un: other
+// blocks still read this block's u for their operator, so u cannot be
+// updated in place.  un then becomes u; the kernel also copies u's halo
+// ring to un, so un is exactly the in-place result.  One FP64 add per cell
+// more in this FP64-bound kernel against a separate pass over u and p:
+// 373.6 -> 350.6 us per iteration at 4096^2 (non-zero fields).
 template <int TH, int F, bool U>
 __device__ __forceinline__ void cheby_block_body(const Dev& d, const Red& red, double alpha,
                                                  double beta, double* un) {
@@ -564,12 +564,6 @@ __device__ __forceinline__ void cheby_block_body(const Dev& d, const Red& red, d
         }
     }
   });
-}
-
-template <int TH, int F>
-__global__ void __launch_bounds__(kBlock, 3)
-    k_cheby_calc_p_block(Dev d, Red red, double alpha, double beta) {
-  cheby_block_body<TH, F, false>(d, red, alpha, beta, nullptr);
 }
 
 template <int TH, int F>
@@ -1180,12 +1174,8 @@ void launch_cheby_init_p(Chunk& c, double theta) {
               div_const(theta), 0.0, 0.0);
 }
 
+// calc_p alone (block Jacobi takes k_cheby_calc_pu_block, with calc_u)
 void launch_cheby_calc_p(Chunk& c, double alpha, double beta) {
-  if (c.prec == PREC_JAC_BLOCK) {
-    TH_DISPATCH(c, "tea_leaf_cheby_solve_calc_p", k_cheby_calc_p_block, c.dev(), c.red(),
-                alpha, beta);
-    return;
-  }
   TH_DISPATCH(c, "tea_leaf_cheby_solve_calc_p", k_cheby_p, c.dev(), c.red(), 1,
               div_const(1.0), alpha, beta);
 }
